@@ -1,0 +1,950 @@
+// Multifrontal sparse LU of the FDFD operator on the GPU.
+//
+// Replaces the factor/solve of pardisoSolver(A, mtype=13) and of scipy's
+// spsolve in solver_direct (fdfdpy/linalg.py:122-149).
+//
+// Storage: every front f of the nested-dissection tree owns a dense
+// column-major ld_f x m_f block in one device pool.  After factorization
+// the block holds
+//   * below the diagonal blocks: L (unit lower, multipliers),
+//   * right of the diagonal blocks: U,
+//   * each nb x nb diagonal block: inv(L_kk) strictly below its diagonal
+//     and inv(U_kk) on and above it (both triangular inverses are used by
+//     the TRSM-as-GEMM updates and by the blocked triangular solves),
+//   * the trailing (m-p) x (m-p) block: the update (Schur complement)
+//     matrix that the parent pulls in by extend-add.
+// The operator is factored scaled by sigma = 1/max|diag(A)| so that the
+// complex64 factor stays well inside float range (Hz entries reach 1e21).
+//
+// Pivoting is static: no row exchanges, and a pivot smaller than
+// sqrt(eps_T) (relative to the scaled operator) is replaced and counted;
+// the FP64 iterative refinement absorbs the perturbation.
+//
+// Parallel schedule: fronts are processed level by level (leaves first).
+// Each launch handles every front of a level: grid.x = front, grid.y/z =
+// tiles of that front.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "cplx.cuh"
+#include "profile.h"
+#include "stencil.cuh"
+
+namespace fdfd {
+
+int norms_device(const void *v, int64_t n, int ncol, double *partial, double *out_dev,
+                 cudaStream_t st);
+size_t norms_partial_count(int ncol);
+int apply_device(const OpDev &o, const void *x, const void *b, void *out, int nrhs, int mode,
+                 cudaStream_t st);
+
+namespace {
+
+constexpr int NB = 64;        // panel width
+constexpr int BM = 64;        // GEMM tile rows
+constexpr int BN = 64;        // GEMM tile cols
+constexpr int BK = 16;        // GEMM K chunk
+constexpr int kRowsPerCta = 256;
+
+struct FrontD {
+    int64_t f_off;  // element offset of the dense block in the pool
+    int32_t m, p, ld, voff;
+    int32_t c0, c1;
+};
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return fail(FDFD_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// max |A[k,k]| over the grid, as the bit pattern of a non-negative double.
+__global__ void k_maxdiag(OpDev o, unsigned long long *out) {
+    const int64_t n = (int64_t)o.Nx * o.Ny;
+    double mx = 0.0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double2 c[5];
+        stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
+        mx = fmax(mx, hypot(c[0].x, c[0].y));
+    }
+    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+}
+
+// Scatter the operator's entries into the fronts: row and column of each
+// pivot variable, restricted to variables of the same front (the entries
+// towards already-eliminated variables were assembled by descendants).
+template <typename T>
+__global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
+                                  const int32_t *__restrict__ var_front,
+                                  const int32_t *__restrict__ var_loc,
+                                  const int32_t *__restrict__ nbr_loc,
+                                  const unsigned long long *maxdiag, T *pool) {
+    const int64_t n = (int64_t)o.Nx * o.Ny;
+    const double sigma = 1.0 / __longlong_as_double((long long)*maxdiag);
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(s / o.Ny), j = (int)(s % o.Ny);
+        const FrontD f = fr[var_front[s]];
+        T *F = pool + f.f_off;
+        const int64_t ld = f.ld;
+        const int k = var_loc[s];
+        double2 c[5];
+        stencil_row(o, i, j, c);
+        F[k + k * ld] = from_c128<T>(c[0], sigma);
+        for (int d = 0; d < 4; ++d) {
+            const int nl = nbr_loc[4 * s + d];
+            if (nl < 0) continue;
+            F[k + nl * ld] = from_c128<T>(c[1 + d], sigma);
+            if (nl >= f.p) {
+                // A[t, s] for the boundary neighbour t: t's coefficient
+                // pointing back towards s.
+                const int t = nbr_cell(o, i, j, d);
+                double2 ct[5];
+                stencil_row(o, t / o.Ny, t % o.Ny, ct);
+                F[nl + k * ld] = from_c128<T>(ct[1 + opposite_dir(d)], sigma);
+            }
+        }
+    }
+}
+
+// Extend-add: the parent pulls child `slot`'s update matrix.
+template <typename T>
+__global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__restrict__ relmap,
+                             T *pool, int f_begin, int slot) {
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int c = slot ? f.c1 : f.c0;
+    if (c < 0) return;
+    const FrontD ch = fr[c];
+    const int mu = ch.m - ch.p;
+    constexpr int CB = 8;
+    const int b0 = blockIdx.y * CB;
+    if (b0 >= mu) return;
+    const int32_t *rm = relmap + ch.voff + ch.p;
+    const T *U = pool + ch.f_off + (int64_t)ch.p * ch.ld + ch.p;
+    T *P = pool + f.f_off;
+    const int64_t ldc = ch.ld, ldp = f.ld;
+    const int bend = min(b0 + CB, mu);
+    for (int b = b0; b < bend; ++b) {
+        const int64_t pc = (int64_t)rm[b] * ldp;
+        for (int a = threadIdx.x; a < mu; a += blockDim.x) {
+            const T u = U[a + b * ldc];
+            T &dst = P[rm[a] + pc];
+            dst = cadd(dst, u);
+        }
+    }
+}
+
+// LU of one nb x nb diagonal block per front (no pivoting), then the two
+// triangular inverses, written back in place.
+template <typename T, typename R>
+__global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, R tiny,
+                          int *tiny_count) {
+    extern __shared__ unsigned char smem_raw[];
+    T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major
+    T *X = D + NB * NB;
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int w = min(NB, f.p - k0);
+    if (w <= 0) return;
+    T *F = pool + f.f_off + (int64_t)k0 * f.ld + k0;
+    const int64_t ld = f.ld;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+        const int r = idx % w, c = idx / w;
+        D[r + c * NB] = F[r + c * ld];
+    }
+    __syncthreads();
+    for (int jj = 0; jj < w; ++jj) {
+        if (tid == 0) {
+            T pv = D[jj + jj * NB];
+            const R a = sqrt(cabs2(pv));
+            if (!(a >= tiny)) {
+                // Static pivot: keep the phase, lift the modulus to tiny.
+                pv = (a > R(0)) ? cmake<R>(pv.x / a * tiny, pv.y / a * tiny) : cmake<R>(tiny, R(0));
+                D[jj + jj * NB] = pv;
+                atomicAdd(tiny_count, 1);
+            }
+        }
+        __syncthreads();
+        const T inv = crecip(D[jj + jj * NB]);
+        for (int r = jj + 1 + tid; r < w; r += blockDim.x) D[r + jj * NB] = cmul(D[r + jj * NB], inv);
+        __syncthreads();
+        const int rem = w - jj - 1;
+        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
+            const int r = jj + 1 + idx % rem, c = jj + 1 + idx / rem;
+            cmsub(D[r + c * NB], D[r + jj * NB], D[jj + c * NB]);
+        }
+        __syncthreads();
+    }
+    // inv(L) column by column (threads 0..w-1), inv(U) row by row
+    // (threads w..2w-1).  Both land in X without overlap.
+    if (tid < w) {
+        const int c = tid;
+        for (int r = c + 1; r < w; ++r) {
+            T acc = D[r + c * NB];
+            for (int t = c + 1; t < r; ++t) cmac(acc, D[r + t * NB], X[t + c * NB]);
+            X[r + c * NB] = cmake<R>(-acc.x, -acc.y);
+        }
+    } else if (tid < 2 * w) {
+        const int r = tid - w;
+        X[r + r * NB] = crecip(D[r + r * NB]);
+        for (int c = r + 1; c < w; ++c) {
+            T acc = czero<T>();
+            for (int t = r; t < c; ++t) cmac(acc, X[r + t * NB], D[t + c * NB]);
+            const T q = cmul(acc, crecip(D[c + c * NB]));
+            X[r + c * NB] = cmake<R>(-q.x, -q.y);
+        }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+        const int r = idx % w, c = idx / w;
+        F[r + c * ld] = X[r + c * NB];
+    }
+}
+
+enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
+
+// Complex SIMT GEMM tile (BM x BN, K = panel width) for the three updates
+// of one panel step:
+//   SCHUR : F[t0:, t0:] -= L[t0:, k0:k0+w] U[k0:k0+w, t0:]
+//   TRSM_L: F[t0:, k0:k0+w] = F[t0:, k0:k0+w] inv(U_kk)      (in place)
+//   TRSM_U: F[k0:k0+w, t0:] = inv(L_kk) F[k0:k0+w, t0:]      (in place)
+// In the in-place modes a CTA owns complete rows (TRSM_L) or columns
+// (TRSM_U) of its output and reads all of them before writing.
+template <typename T, typename R, int MODE>
+__global__ void __launch_bounds__(256) k_gemm(const FrontD *__restrict__ fr, T *pool, int f_begin,
+                                              int k0) {
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int w = min(NB, f.p - k0);
+    if (w <= 0) return;
+    const int t0 = k0 + w;
+    const int m = f.m;
+    int rbase, cbase, rend, cend;
+    if (MODE == SCHUR) {
+        rbase = t0 + blockIdx.y * BM; cbase = t0 + blockIdx.z * BN; rend = m; cend = m;
+    } else if (MODE == TRSM_L) {
+        rbase = t0 + blockIdx.y * BM; cbase = k0; rend = m; cend = t0;
+    } else {
+        rbase = k0; cbase = t0 + blockIdx.z * BN; rend = t0; cend = m;
+    }
+    if (rbase >= rend || cbase >= cend) return;
+    T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = czero<T>();
+
+    for (int kc = 0; kc < w; kc += BK) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int idx = tid + 256 * q;
+            // A tile element (row rr, k kk)
+            {
+                const int rr = idx % BM, kk = idx / BM;
+                const int r = rbase + rr, kg = kc + kk;
+                T v = czero<T>();
+                if (r < rend && kg < w) {
+                    if (MODE == TRSM_U) {
+                        // unit lower inv(L_kk): rows are k0 + rr
+                        const int lr = rr;
+                        if (kg < lr) v = F[(k0 + lr) + (int64_t)(k0 + kg) * ld];
+                        else if (kg == lr) v = cone<T>();
+                    } else {
+                        v = F[r + (int64_t)(k0 + kg) * ld];
+                    }
+                }
+                As[kk][rr] = v;
+            }
+            // B tile element (k kk, col cc)
+            {
+                const int kk = idx % BK, cc = idx / BK;
+                const int c = cbase + cc, kg = kc + kk;
+                T v = czero<T>();
+                if (c < cend && kg < w) {
+                    if (MODE == TRSM_L) {
+                        // upper inv(U_kk): cols are k0 + (c - k0)
+                        const int uc = c - k0;
+                        if (kg <= uc) v = F[(k0 + kg) + (int64_t)c * ld];
+                    } else {
+                        v = F[(k0 + kg) + (int64_t)c * ld];
+                    }
+                }
+                Bs[kk][cc] = v;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T a[4], b[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a[q] = As[kk][ty + 16 * q];
+                b[q] = Bs[kk][tx + 16 * q];
+            }
+#pragma unroll
+            for (int qa = 0; qa < 4; ++qa)
+#pragma unroll
+                for (int qb = 0; qb < 4; ++qb) cmac(acc[qa][qb], a[qa], b[qb]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int qa = 0; qa < 4; ++qa) {
+        const int r = rbase + ty + 16 * qa;
+        if (r >= rend) continue;
+#pragma unroll
+        for (int qb = 0; qb < 4; ++qb) {
+            const int c = cbase + tx + 16 * qb;
+            if (c >= cend) continue;
+            T &dst = F[r + (int64_t)c * ld];
+            if (MODE == SCHUR) dst = csub(dst, acc[qa][qb]);
+            else dst = acc[qa][qb];
+        }
+    }
+}
+
+// ---- solve ------------------------------------------------------------------
+// Workspace layout: W[rhs * sum_m + voff + k] (front-local vectors), Y the
+// same shape (forward solution of the pivot rows).
+
+// Forward, step 1: rhs entries of the pivots and the children's updates.
+template <typename T>
+__global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars,
+                             const int32_t *__restrict__ relmap, const double2 *__restrict__ b,
+                             const double *__restrict__ s_in, T *W, int64_t sum_m, int64_t n,
+                             int nrhs, int f_begin) {
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int32_t *v = vars + f.voff;
+    for (int r = 0; r < nrhs; ++r) {
+        T *w = W + r * sum_m + f.voff;
+        const double s = s_in[r];
+        for (int k = threadIdx.x; k < f.m; k += blockDim.x)
+            w[k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], s) : czero<T>();
+    }
+    __syncthreads();
+    for (int slot = 0; slot < 2; ++slot) {
+        const int c = slot ? f.c1 : f.c0;
+        if (c < 0) continue;
+        const FrontD ch = fr[c];
+        const int mu = ch.m - ch.p;
+        const int32_t *rm = relmap + ch.voff + ch.p;
+        for (int r = 0; r < nrhs; ++r) {
+            T *w = W + r * sum_m + f.voff;
+            const T *wc = W + r * sum_m + ch.voff + ch.p;
+            for (int a = threadIdx.x; a < mu; a += blockDim.x) w[rm[a]] = cadd(w[rm[a]], wc[a]);
+        }
+        __syncthreads();
+    }
+}
+
+// Forward, one panel: y_k = inv(L_kk) w_k (every CTA of the front computes
+// it; CTA 0 stores it to Y), then w[t0:m] -= L[t0:m, k] y_k.
+template <typename T, typename R>
+__global__ void k_fwd_panel(const FrontD *__restrict__ fr, const T *__restrict__ pool, T *W, T *Y,
+                            int64_t sum_m, int nrhs, int f_begin, int k0) {
+    extern __shared__ unsigned char smem_raw[];
+    T *yk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int w = min(NB, f.p - k0);
+    if (w <= 0) return;
+    const int t0 = k0 + w;
+    const int rbase = t0 + blockIdx.y * kRowsPerCta;
+    if (blockIdx.y > 0 && rbase >= f.m) return;
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+        const int r = idx / w, row = idx % w;
+        const T *wv = W + r * sum_m + f.voff + k0;
+        T acc = wv[row];
+        for (int t = 0; t < row; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], wv[t]);
+        yk[r * NB + row] = acc;
+    }
+    __syncthreads();
+    if (blockIdx.y == 0)
+        for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+            const int r = idx / w, row = idx % w;
+            Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
+        }
+    const int row = rbase + tid;
+    if (row < f.m) {
+        for (int r = 0; r < nrhs; ++r) {
+            T acc = czero<T>();
+            for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], yk[r * NB + t]);
+            T &dst = W[r * sum_m + f.voff + row];
+            dst = csub(dst, acc);
+        }
+    }
+}
+
+// Backward, step 1: acc[0:p] = y[0:p] - U[0:p, p:m] x_B, x_B read from the
+// global solution (ancestors are already solved).
+template <typename T>
+__global__ void k_bwd_init(const FrontD *__restrict__ fr, const T *__restrict__ pool,
+                           const int32_t *__restrict__ vars, T *W, const T *__restrict__ Y,
+                           const double2 *__restrict__ x, const double *__restrict__ s_in,
+                           int64_t sum_m, int64_t n, int nrhs, int f_begin, int max_nrhs) {
+    extern __shared__ unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int row = blockIdx.y * kRowsPerCta + threadIdx.x;
+    if (blockIdx.y * kRowsPerCta >= f.p) return;
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int32_t *v = vars + f.voff;
+    T acc[8];
+    for (int r = 0; r < nrhs; ++r)
+        acc[r] = (row < f.p) ? Y[r * sum_m + f.voff + row] : czero<T>();
+    for (int c0 = f.p; c0 < f.m; c0 += kRowsPerCta) {
+        const int cn = min(kRowsPerCta, f.m - c0);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < cn * nrhs; idx += blockDim.x) {
+            const int r = idx / cn, cc = idx % cn;
+            xs[r * kRowsPerCta + cc] = from_c128<T>(x[r * n + v[c0 + cc]], s_in[r]);
+        }
+        __syncthreads();
+        if (row < f.p)
+            for (int cc = 0; cc < cn; ++cc) {
+                const T a = F[row + (int64_t)(c0 + cc) * ld];
+                for (int r = 0; r < nrhs; ++r) cmsub(acc[r], a, xs[r * kRowsPerCta + cc]);
+            }
+    }
+    if (row < f.p)
+        for (int r = 0; r < nrhs; ++r) W[r * sum_m + f.voff + row] = acc[r];
+    (void)max_nrhs;
+}
+
+// Backward, one panel (descending k): x_k = inv(U_kk) acc_k, CTA 0 writes
+// x_k to the global solution, then acc[0:k0] -= U[0:k0, k] x_k.
+template <typename T, typename R>
+__global__ void k_bwd_panel(const FrontD *__restrict__ fr, const T *__restrict__ pool,
+                            const int32_t *__restrict__ vars, T *W, double2 *x,
+                            const double *__restrict__ s_out, int64_t sum_m, int64_t n, int nrhs,
+                            int f_begin, int k0) {
+    extern __shared__ unsigned char smem_raw[];
+    T *xk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int w = min(NB, f.p - k0);
+    if (w <= 0) return;
+    const int rbase = blockIdx.y * kRowsPerCta;
+    if (blockIdx.y > 0 && rbase >= k0) return;
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+        const int r = idx / w, row = idx % w;
+        const T *av = W + r * sum_m + f.voff + k0;
+        T acc = czero<T>();
+        for (int t = row; t < w; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], av[t]);
+        xk[r * NB + row] = acc;
+    }
+    __syncthreads();
+    if (blockIdx.y == 0) {
+        const int32_t *v = vars + f.voff + k0;
+        for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+            const int r = idx / w, row = idx % w;
+            x[r * n + v[row]] = to_c128(xk[r * NB + row], s_out[r]);
+        }
+    }
+    const int row = rbase + tid;
+    if (row < k0) {
+        for (int r = 0; r < nrhs; ++r) {
+            T acc = czero<T>();
+            for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], xk[r * NB + t]);
+            T &dst = W[r * sum_m + f.voff + row];
+            dst = csub(dst, acc);
+        }
+    }
+}
+
+// Per-column solve scales: s_in = 1/||r||, s_out = sigma ||r||.
+__global__ void k_scales(const double *norms, const unsigned long long *maxdiag, int nrhs,
+                         double *s_in, double *s_out) {
+    const int r = threadIdx.x;
+    if (r >= nrhs) return;
+    const double nr = norms[r];
+    const double sigma = 1.0 / __longlong_as_double((long long)*maxdiag);
+    if (nr > 0.0 && isfinite(nr)) {
+        s_in[r] = 1.0 / nr;
+        s_out[r] = sigma * nr;
+    } else {
+        s_in[r] = 0.0;
+        s_out[r] = 0.0;
+    }
+}
+
+// P-scaling for transposed solves: P = diag(sxf(i) syf(j)) makes P A
+// complex symmetric, so A^T = P A P^-1 and A^-T g = P A^-1 P^-1 g.
+// mode 0: out = P^-1 in (multiply by inv_sxf inv_syf); mode 1: out = P in.
+__global__ void k_pscale(const double2 *in, double2 *out, const double2 *isxf, const double2 *isyf,
+                         int Nx, int Ny, int nrhs, int mode) {
+    const int64_t n = (int64_t)Nx * Ny;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n * nrhs;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = k % n;
+        const int i = (int)(c / Ny), j = (int)(c % Ny);
+        const double2 a = isxf[i], b = isyf[j];
+        double2 q = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        if (mode == 1) {
+            const double d = q.x * q.x + q.y * q.y;
+            q = make_double2(q.x / d, -q.y / d);
+        }
+        const double2 v = in[k];
+        out[k] = make_double2(v.x * q.x - v.y * q.y, v.x * q.y + v.y * q.x);
+    }
+}
+
+__global__ void k_axpy(double2 *x, const double2 *d, int64_t len) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < len;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const double2 a = x[k], b = d[k];
+        x[k] = make_double2(a.x + b.x, a.y + b.y);
+    }
+}
+
+inline int grid1(int64_t n) {
+    int64_t b = (n + 255) / 256;
+    if (b < 1) b = 1;
+    if (b > 152 * 32) b = 152 * 32;
+    return (int)b;
+}
+
+}  // namespace
+}  // namespace fdfd
+
+// ---------------------------------------------------------------------------
+// Factor handle.
+using namespace fdfd;
+
+struct fdfd_factor {
+    fdfd_symbolic *sym = nullptr;
+    int precision = FDFD_PREC_C128;
+    int max_nrhs = 1;
+    int device = 0;
+    size_t elem = 16;
+    int64_t n = 0;
+    // device arrays
+    FrontD *d_fronts = nullptr;
+    int32_t *d_vars = nullptr, *d_relmap = nullptr, *d_nbr = nullptr, *d_vfront = nullptr,
+            *d_vloc = nullptr;
+    void *d_pool = nullptr, *d_W = nullptr, *d_Y = nullptr;
+    double2 *d_r = nullptr, *d_d = nullptr, *d_tmp = nullptr;
+    double2 *d_isxf = nullptr, *d_isyf = nullptr;
+    double *d_partial = nullptr, *d_norm = nullptr, *d_sin = nullptr, *d_sout = nullptr,
+           *d_unit = nullptr;
+    unsigned long long *d_maxdiag = nullptr;
+    int *d_tiny = nullptr;
+    double *h_norm = nullptr;  // pinned
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool numeric_done = false;
+    int Nx = 0, Ny = 0;
+    fdfd_factor_stats stats{};
+};
+
+namespace fdfd {
+namespace {
+
+template <typename T, typename R>
+int set_smem_attrs() {
+    CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * NB * NB * sizeof(T))));
+    return FDFD_OK;
+}
+
+template <typename T, typename R>
+int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
+    const Symbolic &S = fac->sym->s;
+    CUDA_TRY(cudaMemsetAsync(fac->d_pool, 0, (size_t)S.pool_entries * sizeof(T), st));
+    CUDA_TRY(cudaMemsetAsync(fac->d_tiny, 0, sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(fac->d_maxdiag, 0, sizeof(unsigned long long), st));
+    prof_begin(PROF_ASSEMBLE, st);
+    k_maxdiag<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_maxdiag);
+    k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc,
+                                                       fac->d_nbr, fac->d_maxdiag, (T *)fac->d_pool);
+    prof_end(PROF_ASSEMBLE, st, 2);
+    const R tiny = (R)std::sqrt((double)std::numeric_limits<R>::epsilon());
+    T *pool = (T *)fac->d_pool;
+    for (int L = 0; L < S.nlev; ++L) {
+        const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
+        if (L > 0) {
+            int maxmu = 0;
+            for (int f = fb; f < fb + nfl; ++f) {
+                const int cs[2] = {S.child0[f], S.child1[f]};
+                for (int c : cs)
+                    if (c >= 0) maxmu = std::max(maxmu, S.m[c] - S.p[c]);
+            }
+            if (maxmu > 0) {
+                dim3 g(nfl, (maxmu + 7) / 8);
+                prof_begin(PROF_EXTEND_ADD, st);
+                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 0);
+                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 1);
+                prof_end(PROF_EXTEND_ADD, st, 2);
+            }
+        }
+        const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
+        for (int k0 = 0; k0 < maxp; k0 += NB) {
+            prof_begin(PROF_LU_DIAG, st);
+            k_lu_diag<T, R><<<nfl, 256, 2 * NB * NB * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
+                                                                       tiny, fac->d_tiny);
+            prof_end(PROF_LU_DIAG, st, 1);
+            const int trail = maxm - k0 - 1;  // upper bound of m - t0
+            if (trail <= 0) continue;
+            const int tiles = (trail + BM - 1) / BM;
+            prof_begin(PROF_TRSM, st);
+            k_gemm<T, R, TRSM_L><<<dim3(nfl, tiles, 1), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+            k_gemm<T, R, TRSM_U><<<dim3(nfl, 1, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+            prof_end(PROF_TRSM, st, 2);
+            prof_begin(PROF_SCHUR, st);
+            k_gemm<T, R, SCHUR><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+            prof_end(PROF_SCHUR, st, 1);
+        }
+    }
+    CUDA_TRY(cudaGetLastError());
+    return FDFD_OK;
+}
+
+// x = A^-1 b for nrhs columns (b, x complex128 on device; may alias d_tmp).
+// s_in / s_out are device arrays of per-column scales.
+template <typename T, typename R>
+int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaStream_t st) {
+    const Symbolic &S = fac->sym->s;
+    T *W = (T *)fac->d_W, *Y = (T *)fac->d_Y;
+    const T *pool = (const T *)fac->d_pool;
+    const int64_t sum_m = S.sum_m, n = fac->n;
+    const size_t sm_panel = (size_t)nrhs * NB * sizeof(T);
+    for (int L = 0; L < S.nlev; ++L) {
+        const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
+        prof_begin(PROF_SOLVE_FWD, st);
+        k_fwd_gather<T><<<nfl, 256, 0, st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, b, fac->d_unit,
+                                             W, sum_m, n, nrhs, fb);
+        const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
+        int nl = 1;
+        for (int k0 = 0; k0 < maxp; k0 += NB, ++nl) {
+            const int rows = std::max(1, (maxm - k0 + kRowsPerCta - 1) / kRowsPerCta);
+            k_fwd_panel<T, R><<<dim3(nfl, rows), kRowsPerCta, sm_panel, st>>>(fac->d_fronts, pool, W, Y,
+                                                                            sum_m, nrhs, fb, k0);
+        }
+        prof_end(PROF_SOLVE_FWD, st, nl);
+    }
+    for (int L = S.nlev - 1; L >= 0; --L) {
+        const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
+        const int maxp = S.lev_max_p[L];
+        const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
+        prof_begin(PROF_SOLVE_BWD, st);
+        k_bwd_init<T><<<dim3(nfl, prow), kRowsPerCta, (size_t)nrhs * kRowsPerCta * sizeof(T), st>>>(
+            fac->d_fronts, pool, fac->d_vars, W, Y, x, fac->d_unit, sum_m, n, nrhs, fb, fac->max_nrhs);
+        int nl = 1;
+        for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB, ++nl) {
+            const int rows = std::max(1, (k0 + kRowsPerCta - 1) / kRowsPerCta);
+            k_bwd_panel<T, R><<<dim3(nfl, rows), kRowsPerCta, sm_panel, st>>>(
+                fac->d_fronts, pool, fac->d_vars, W, x, fac->d_unit, sum_m, n, nrhs, fb, k0);
+        }
+        prof_end(PROF_SOLVE_BWD, st, nl);
+    }
+    CUDA_TRY(cudaGetLastError());
+    return FDFD_OK;
+}
+
+}  // namespace
+}  // namespace fdfd
+
+// The backward phase works in the scaled unknowns y = x / s_out; the global
+// x written by k_bwd_panel must therefore stay in scaled units until every
+// level is done (ancestors' x is read back by k_bwd_init).  The solve runs
+// with unit scales internally and applies s_in / s_out around it.
+namespace fdfd {
+namespace {
+
+__global__ void k_colscale(const double2 *in, double2 *out, const double *s, int64_t n, int nrhs) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n * nrhs;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const double c = s[k / n];
+        const double2 v = in[k];
+        out[k] = make_double2(v.x * c, v.y * c);
+    }
+}
+
+// One application of the factor on device vectors (no host sync):
+// out = A^-1 in  (transpose = 0) or A^-T in (transpose = 1).
+int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, int transpose,
+                 cudaStream_t st) {
+    const int64_t n = fac->n;
+    double2 *tmp = fac->d_tmp;
+    const double2 *src = in;
+    if (transpose) {
+        k_pscale<<<grid1(n * nrhs), 256, 0, st>>>(in, tmp, fac->d_isxf, fac->d_isyf, fac->Nx, fac->Ny,
+                                                  nrhs, 0);
+        src = tmp;
+    }
+    // scales from the column norms of the right-hand side
+    prof_begin(PROF_OTHER, st);
+    int rc = norms_device(src, n, nrhs, fac->d_partial, fac->d_norm, st);
+    if (rc) return rc;
+    k_scales<<<1, 32, 0, st>>>(fac->d_norm, fac->d_maxdiag, nrhs, fac->d_sin, fac->d_sout);
+    k_colscale<<<grid1(n * nrhs), 256, 0, st>>>(src, tmp, fac->d_sin, n, nrhs);
+    prof_end(PROF_OTHER, st, 4 + (transpose ? 1 : 0));
+    if (fac->precision == FDFD_PREC_C64)
+        rc = solve_levels<c64, float>(fac, tmp, out, nrhs, st);
+    else
+        rc = solve_levels<c128, double>(fac, tmp, out, nrhs, st);
+    if (rc) return rc;
+    prof_begin(PROF_OTHER, st);
+    k_colscale<<<grid1(n * nrhs), 256, 0, st>>>(out, out, fac->d_sout, n, nrhs);
+    prof_end(PROF_OTHER, st, 1 + (transpose ? 1 : 0));
+    if (transpose)
+        k_pscale<<<grid1(n * nrhs), 256, 0, st>>>(out, out, fac->d_isxf, fac->d_isyf, fac->Nx, fac->Ny,
+                                                  nrhs, 1);
+    CUDA_TRY(cudaGetLastError());
+    return FDFD_OK;
+}
+
+void free_factor(fdfd_factor *f) {
+    if (!f) return;
+    void *ptrs[] = {f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
+                    f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
+                    f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (f->h_norm) cudaFreeHost(f->h_norm);
+    for (auto &e : f->ev)
+        if (e) cudaEventDestroy(e);
+    delete f;
+}
+
+int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
+    const int64_t elem = precision == FDFD_PREC_C64 ? 8 : 16;
+    const int64_t n = (int64_t)S.Nx * S.Ny;
+    int64_t b = S.pool_entries * elem;
+    b += 2 * S.sum_m * max_nrhs * elem;                  // W, Y
+    b += 3 * n * max_nrhs * 16;                          // r, d, tmp
+    b += (int64_t)S.nf * sizeof(FrontD);
+    b += 2 * S.sum_m * 4 + 6 * n * 4;                    // vars, relmap, nbr, var maps
+    b += (int64_t)(S.Nx + S.Ny) * 16;
+    b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
+    return b;
+}
+
+}  // namespace
+}  // namespace fdfd
+
+extern "C" int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision, int32_t max_nrhs,
+                                 int64_t *bytes) {
+    if (!sym || !bytes) return fail(FDFD_ERR_BAD_ARG, "factor_bytes: NULL argument");
+    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64)
+        return fail(FDFD_ERR_BAD_ARG, "factor_bytes: unknown precision");
+    if (max_nrhs < 1 || max_nrhs > 8) return fail(FDFD_ERR_BAD_ARG, "factor_bytes: max_nrhs must be 1..8");
+    *bytes = factor_bytes_of(sym->s, precision, max_nrhs);
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t max_nrhs,
+                                  fdfd_factor **out) {
+    if (!sym || !out) return fail(FDFD_ERR_BAD_ARG, "factor_create: NULL argument");
+    *out = nullptr;
+    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64)
+        return fail(FDFD_ERR_BAD_ARG, "factor_create: unknown precision");
+    if (max_nrhs < 1 || max_nrhs > 8) return fail(FDFD_ERR_BAD_ARG, "factor_create: max_nrhs must be 1..8");
+    const Symbolic &S = sym->s;
+    if (S.Nx < 3 || S.Ny < 3) return fail(FDFD_ERR_BAD_ARG, "factor_create: grid must be at least 3x3");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail(FDFD_ERR_NO_DEVICE, "factor_create: no CUDA device");
+    }
+    fdfd_factor *f = new fdfd_factor();
+    f->sym = sym;
+    f->precision = precision;
+    f->max_nrhs = max_nrhs;
+    f->elem = precision == FDFD_PREC_C64 ? 8 : 16;
+    f->n = (int64_t)S.Nx * S.Ny;
+    f->Nx = S.Nx;
+    f->Ny = S.Ny;
+    cudaGetDevice(&f->device);
+
+    std::vector<FrontD> fd(S.nf);
+    for (int i = 0; i < S.nf; ++i) {
+        fd[i].f_off = S.pool_off[i];
+        fd[i].m = S.m[i];
+        fd[i].p = S.p[i];
+        fd[i].ld = S.ld[i];
+        fd[i].voff = S.vars_off[i];
+        fd[i].c0 = S.child0[i];
+        fd[i].c1 = S.child1[i];
+    }
+    auto alloc = [&](void **p, size_t bytes) -> bool {
+        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
+    };
+    const int64_t n = f->n;
+    bool ok = alloc((void **)&f->d_fronts, S.nf * sizeof(FrontD)) &&
+              alloc((void **)&f->d_vars, S.sum_m * 4) && alloc((void **)&f->d_relmap, S.sum_m * 4) &&
+              alloc((void **)&f->d_nbr, 4 * n * 4) && alloc((void **)&f->d_vfront, n * 4) &&
+              alloc((void **)&f->d_vloc, n * 4) && alloc(&f->d_pool, S.pool_entries * f->elem) &&
+              alloc(&f->d_W, S.sum_m * max_nrhs * f->elem) &&
+              alloc(&f->d_Y, S.sum_m * max_nrhs * f->elem) &&
+              alloc((void **)&f->d_r, n * max_nrhs * 16) && alloc((void **)&f->d_d, n * max_nrhs * 16) &&
+              alloc((void **)&f->d_tmp, n * max_nrhs * 16) && alloc((void **)&f->d_isxf, S.Nx * 16) &&
+              alloc((void **)&f->d_isyf, S.Ny * 16) &&
+              alloc((void **)&f->d_partial, norms_partial_count(max_nrhs) * 8) &&
+              alloc((void **)&f->d_norm, max_nrhs * 8) && alloc((void **)&f->d_sin, max_nrhs * 8) &&
+              alloc((void **)&f->d_sout, max_nrhs * 8) && alloc((void **)&f->d_unit, 8 * 8) &&
+              alloc((void **)&f->d_maxdiag, 8) && alloc((void **)&f->d_tiny, 4);
+    if (!ok) {
+        free_factor(f);
+        return fail(FDFD_ERR_OOM, "factor_create: device allocation failed");
+    }
+    cudaError_t e = cudaMallocHost((void **)&f->h_norm, 8 * sizeof(double));
+    for (auto &ev : f->ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    const double ones[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_fronts, fd.data(), S.nf * sizeof(FrontD), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_vars, S.vars.data(), S.sum_m * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_relmap, S.relmap.data(), S.sum_m * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_nbr, S.nbr_loc.data(), 4 * n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_vfront, S.var_front.data(), n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_vloc, S.var_loc.data(), n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(f->d_unit, ones, sizeof(ones), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        free_factor(f);
+        return fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+    }
+    int rc = (precision == FDFD_PREC_C64) ? set_smem_attrs<c64, float>() : set_smem_attrs<c128, double>();
+    if (rc) {
+        free_factor(f);
+        return rc;
+    }
+    *out = f;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, void *stream) {
+    if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_numeric: NULL factor");
+    OpDev o;
+    int rc = make_opdev(op, &o);
+    if (rc) return rc;
+    if (op->Nx != fac->Nx || op->Ny != fac->Ny)
+        return fail(FDFD_ERR_BAD_ARG, "factor_numeric: operator grid differs from the symbolic grid");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(fac->d_isxf, op->inv_sxf, fac->Nx * 16, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(fac->d_isyf, op->inv_syf, fac->Ny * 16, cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(cudaEventRecord(fac->ev[0], st));
+    rc = (fac->precision == FDFD_PREC_C64) ? factor_levels<c64, float>(fac, o, st)
+                                           : factor_levels<c128, double>(fac, o, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(fac->ev[1], st));
+    fac->numeric_done = true;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x, int32_t nrhs,
+                                 int32_t transpose, void *stream) {
+    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "factor_solve: NULL argument");
+    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "factor_solve: factor has no numeric values");
+    if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "factor_solve: nrhs out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaEventRecord(fac->ev[2], st));
+    int rc = apply_factor(fac, (const double2 *)b, (double2 *)x, nrhs, transpose, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(fac->ev[3], st));
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, const void *b, void *x,
+                                  int32_t nrhs, int32_t transpose, double tol, int32_t max_iter,
+                                  void *stream) {
+    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_refined: NULL argument");
+    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_refined: factor has no numeric values");
+    if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "solve_refined: nrhs out of range");
+    if (max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_refined: max_iter must be >= 0");
+    OpDev o;
+    int rc = make_opdev(op, &o);
+    if (rc) return rc;
+    if (op->Nx != fac->Nx || op->Ny != fac->Ny)
+        return fail(FDFD_ERR_BAD_ARG, "solve_refined: operator grid differs from the factor grid");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = fac->n;
+    const double2 *bb = (const double2 *)b;
+    double2 *xx = (double2 *)x;
+    CUDA_TRY(cudaEventRecord(fac->ev[2], st));
+    double bnorm[8];
+    prof_begin(PROF_OTHER, st);
+    rc = norms_device(bb, n, nrhs, fac->d_partial, fac->d_norm, st);
+    if (rc) return rc;
+    prof_end(PROF_OTHER, st, 2);
+    CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for (int r = 0; r < nrhs; ++r) bnorm[r] = fac->h_norm[r];
+    rc = apply_factor(fac, bb, xx, nrhs, transpose, st);
+    if (rc) return rc;
+    double worst = 0.0;
+    int it = 0;
+    for (;;) {
+        // r = b - A x (or b - A^T x), FP64, matrix-free
+        prof_begin(PROF_OTHER, st);
+        rc = apply_device(o, xx, bb, fac->d_r, nrhs, transpose ? 3 : 0, st);
+        if (rc) return rc;
+        rc = norms_device(fac->d_r, n, nrhs, fac->d_partial, fac->d_norm, st);
+        if (rc) return rc;
+        prof_end(PROF_OTHER, st, 3);
+        CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        worst = 0.0;
+        for (int r = 0; r < nrhs; ++r) {
+            const double rel = bnorm[r] > 0 ? fac->h_norm[r] / bnorm[r] : fac->h_norm[r];
+            worst = std::max(worst, rel);
+        }
+        if (!(worst > tol) || it >= max_iter) break;
+        rc = apply_factor(fac, fac->d_r, fac->d_d, nrhs, transpose, st);
+        if (rc) return rc;
+        prof_begin(PROF_OTHER, st);
+        k_axpy<<<grid1(n * nrhs), 256, 0, st>>>(xx, fac->d_d, n * nrhs);
+        prof_end(PROF_OTHER, st, 1);
+        ++it;
+    }
+    CUDA_TRY(cudaEventRecord(fac->ev[3], st));
+    fac->stats.refine_iters = it;
+    fac->stats.rel_residual = worst;
+    if (!(worst <= tol))
+        return fail(FDFD_ERR_NOT_CONVERGED, "solve_refined: residual " + std::to_string(worst) +
+                                                " above tolerance after " + std::to_string(it) +
+                                                " refinement steps");
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st) {
+    if (!fac || !st) return fail(FDFD_ERR_BAD_ARG, "factor_stats: NULL argument");
+    fdfd_factor *f = const_cast<fdfd_factor *>(fac);
+    float ms = 0.f;
+    if (f->numeric_done && cudaEventSynchronize(f->ev[1]) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, f->ev[0], f->ev[1]) == cudaSuccess)
+        f->stats.factor_ms = ms;
+    if (cudaEventQuery(f->ev[3]) == cudaSuccess && cudaEventElapsedTime(&ms, f->ev[2], f->ev[3]) == cudaSuccess)
+        f->stats.solve_ms = ms;
+    cudaGetLastError();
+    int tiny = 0;
+    if (f->numeric_done && cudaMemcpy(&tiny, f->d_tiny, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
+        f->stats.tiny_pivots = tiny;
+    *st = f->stats;
+    return FDFD_OK;
+}
+
+extern "C" void fdfd_factor_destroy(fdfd_factor *fac) { free_factor(fac); }

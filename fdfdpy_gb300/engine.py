@@ -1,0 +1,296 @@
+"""Device-side objects of the engine: operators, symbolic analyses, factors.
+
+Device memory for operator inputs and right-hand sides is held in torch
+tensors (torch is used for allocation and streams only); every computation
+is a call into the engine's CUDA library through its C ABI.  Nothing here
+computes on the CPU besides O(1) bookkeeping; a machine without a CUDA
+device gets an error, not a slower path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _native as N
+from .constants import DEFAULT_LEAF_AREA
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise N.FDFDError(N.FDFD_ERR_NO_DEVICE, "the FDFD engine needs a CUDA device (no CPU fallback)")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def as_c128(x, shape=None) -> torch.Tensor:
+    """Host/device array -> contiguous complex128 device tensor."""
+    dev = device()
+    if isinstance(x, torch.Tensor):
+        t = x.to(device=dev, dtype=torch.complex128)
+    else:
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
+        t = torch.from_numpy(a).to(dev, non_blocking=False)
+    t = t.contiguous()
+    return t if shape is None else t.reshape(shape)
+
+
+def as_f64(x) -> torch.Tensor:
+    dev = device()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=torch.float64).contiguous()
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    return torch.from_numpy(a).to(dev)
+
+
+class DeviceOperator:
+    """The PML-stretched operator of one (omega, eps_r, dl, NPML, pol, L0)
+    on the device: eps_r, the four 1/s vectors (computed on the GPU) and the
+    C-ABI operator struct pointing at them.  Mirrors the inputs of
+    construct_A (fdfdpy/linalg.py:41-44)."""
+
+    def __init__(self, omega, eps_r, xlen, ylen, NPML, pol, L0, averaging=True,
+                 eps_add=None, diag_add=None):
+        if pol not in N.POL:
+            raise ValueError(f"Invalid polarization: {pol}")
+        eps = eps_r if isinstance(eps_r, torch.Tensor) else np.asarray(eps_r, dtype=np.float64)
+        if eps.ndim != 2:
+            raise ValueError("eps_r must be a 2-D array")
+        self.Nx, self.Ny = int(eps.shape[0]), int(eps.shape[1])
+        if self.Nx < 3 or self.Ny < 3:
+            raise ValueError("the GPU operator needs a grid of at least 3 x 3 cells")
+        self.omega, self.L0, self.pol = float(omega), float(L0), pol
+        self.xlen, self.ylen = float(xlen), float(ylen)
+        self.NPML = [int(NPML[0]), int(NPML[1])]
+        self.averaging = bool(averaging)
+        self.eps = as_f64(eps).reshape(-1)
+        self.eps_add = None if eps_add is None else as_f64(eps_add).reshape(-1)
+        self.diag_add = None if diag_add is None else as_c128(diag_add).reshape(-1)
+        dev = device()
+        self.inv_s = [torch.empty(self.Nx, dtype=torch.complex128, device=dev),
+                      torch.empty(self.Nx, dtype=torch.complex128, device=dev),
+                      torch.empty(self.Ny, dtype=torch.complex128, device=dev),
+                      torch.empty(self.Ny, dtype=torch.complex128, device=dev)]
+        st = stream_ptr()
+        N.call("fdfd_pml_sfactors", self.Nx, self.NPML[0], self.xlen, self.omega, self.L0,
+               _ptr(self.inv_s[0]), _ptr(self.inv_s[1]), st)
+        N.call("fdfd_pml_sfactors", self.Ny, self.NPML[1], self.ylen, self.omega, self.L0,
+               _ptr(self.inv_s[2]), _ptr(self.inv_s[3]), st)
+
+    @property
+    def n(self):
+        return self.Nx * self.Ny
+
+    def struct(self, averaging=None, eps=None, eps_add="keep", diag_add="keep") -> N.Operator:
+        op = N.Operator()
+        op.Nx, op.Ny, op.pol = self.Nx, self.Ny, N.POL[self.pol]
+        op.averaging = int(self.averaging if averaging is None else averaging)
+        op.omega, op.L0, op.xlen, op.ylen = self.omega, self.L0, self.xlen, self.ylen
+        op.eps = (self.eps if eps is None else eps).data_ptr()
+        ea = self.eps_add if isinstance(eps_add, str) else eps_add
+        da = self.diag_add if isinstance(diag_add, str) else diag_add
+        op.eps_add = None if ea is None else ea.data_ptr()
+        op.diag_add = None if da is None else da.data_ptr()
+        op.inv_sxf, op.inv_sxb, op.inv_syf, op.inv_syb = (t.data_ptr() for t in self.inv_s)
+        self._keep = (ea, da)
+        return op
+
+    def with_terms(self, eps_add=None, diag_add=None) -> "DeviceOperator":
+        """Same operator with a diagonal Kerr term / complex diagonal added."""
+        o = object.__new__(DeviceOperator)
+        o.__dict__.update(self.__dict__)
+        o.eps_add = None if eps_add is None else as_f64(eps_add).reshape(-1)
+        o.diag_add = None if diag_add is None else as_c128(diag_add).reshape(-1)
+        return o
+
+    # ---- K1 -----------------------------------------------------------------
+    def csr_device(self):
+        dev = device()
+        n = self.n
+        indptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        indices = torch.empty(5 * n, dtype=torch.int32, device=dev)
+        data = torch.empty(5 * n, dtype=torch.complex128, device=dev)
+        op = self.struct()
+        N.call("fdfd_assemble_csr", C.byref(op), _ptr(indptr), _ptr(indices), _ptr(data), stream_ptr())
+        return indptr, indices, data
+
+    def csr(self) -> sp.csr_matrix:
+        indptr, indices, data = self.csr_device()
+        n = self.n
+        return sp.csr_matrix((data.cpu().numpy(), indices.cpu().numpy(), indptr.cpu().numpy()),
+                             shape=(n, n))
+
+    def deriv_csr(self, which: str) -> sp.csr_matrix:
+        code = {"Dxf": 0, "Dxb": 1, "Dyf": 2, "Dyb": 3}[which]
+        dev = device()
+        n = self.n
+        indptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+        indices = torch.empty(2 * n, dtype=torch.int32, device=dev)
+        data = torch.empty(2 * n, dtype=torch.complex128, device=dev)
+        op = self.struct()
+        N.call("fdfd_assemble_deriv_csr", C.byref(op), code, _ptr(indptr), _ptr(indices), _ptr(data),
+               stream_ptr())
+        return sp.csr_matrix((data.cpu().numpy(), indices.cpu().numpy(), indptr.cpu().numpy()),
+                             shape=(n, n))
+
+    # ---- K2 -----------------------------------------------------------------
+    def residual(self, x, b):
+        x = as_c128(x)
+        b = as_c128(b)
+        nrhs = x.numel() // self.n
+        r = torch.empty_like(b)
+        op = self.struct()
+        N.call("fdfd_residual", C.byref(op), _ptr(x), _ptr(b), _ptr(r), nrhs, stream_ptr())
+        return r
+
+    def apply(self, x, transpose=False):
+        x = as_c128(x)
+        nrhs = x.numel() // self.n
+        y = torch.empty_like(x)
+        op = self.struct()
+        N.call("fdfd_apply", C.byref(op), _ptr(x), _ptr(y), nrhs, int(bool(transpose)), stream_ptr())
+        return y
+
+    # ---- K8 -----------------------------------------------------------------
+    def fields(self, X, averaging=True, eps=None):
+        X = as_c128(X).reshape(-1)
+        f1 = torch.empty_like(X)
+        f2 = torch.empty_like(X)
+        op = self.struct(averaging=averaging, eps=eps)
+        N.call("fdfd_fields", C.byref(op), _ptr(X), _ptr(f1), _ptr(f2), stream_ptr())
+        return f1, f2
+
+    # ---- K9 -----------------------------------------------------------------
+    def grad_eps(self, lam, E):
+        lam = as_c128(lam).reshape(-1)
+        E = as_c128(E).reshape(-1)
+        g = torch.empty(self.n, dtype=torch.float64, device=lam.device)
+        op = self.struct()
+        N.call("fdfd_adjoint_grad_eps", C.byref(op), _ptr(lam), _ptr(E), _ptr(g), stream_ptr())
+        return g
+
+
+def norms(v: torch.Tensor, n: int):
+    v = as_c128(v)
+    ncol = v.numel() // n
+    out = (C.c_double * ncol)()
+    N.call("fdfd_norms", _ptr(v), n, ncol, out, stream_ptr())
+    return np.array(out[:])
+
+
+class Symbolic:
+    """Nested-dissection front tree of an Nx x Ny periodic grid (host)."""
+
+    def __init__(self, Nx, Ny, leaf_area=DEFAULT_LEAF_AREA):
+        h = C.c_void_p()
+        N.call("fdfd_symbolic_create", int(Nx), int(Ny), int(leaf_area), C.byref(h))
+        self.handle = h
+        self.Nx, self.Ny, self.leaf_area = int(Nx), int(Ny), int(leaf_area)
+        info = N.SymbolicInfo()
+        N.call("fdfd_symbolic_info_get", h, C.byref(info))
+        self.info = info
+
+    def export(self, which: int, count: int, dtype=np.int32):
+        out = np.empty(count, dtype=dtype)
+        N.call("fdfd_symbolic_export", self.handle, which, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def __del__(self):
+        try:
+            if self.handle:
+                N.lib().fdfd_symbolic_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+_sym_cache: dict = {}
+_sym_lock = threading.Lock()
+
+
+def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
+    """Symbolic analyses are cached per grid shape (they depend on nothing else)."""
+    key = (int(Nx), int(Ny), int(leaf_area))
+    with _sym_lock:
+        s = _sym_cache.get(key)
+        if s is None:
+            s = Symbolic(*key)
+            _sym_cache[key] = s
+        return s
+
+
+class Factor:
+    """A numeric multifrontal factorization of one operator on the device."""
+
+    def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1):
+        if precision not in N.PREC:
+            raise ValueError("precision must be 'c128' or 'c64'")
+        device()
+        self.sym, self.precision, self.max_nrhs = sym, precision, int(max_nrhs)
+        h = C.c_void_p()
+        N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
+        self.handle = h
+        self.op = None
+
+    @staticmethod
+    def bytes_needed(sym: Symbolic, precision="c128", max_nrhs=1) -> int:
+        b = C.c_int64()
+        N.call("fdfd_factor_bytes", sym.handle, N.PREC[precision], int(max_nrhs), C.byref(b))
+        return int(b.value)
+
+    def numeric(self, op: DeviceOperator):
+        s = op.struct()
+        N.call("fdfd_factor_numeric", self.handle, C.byref(s), stream_ptr())
+        self.op = op
+        self._op_struct = s
+        return self
+
+    def apply_inverse(self, b, transpose=False):
+        """One application x = A^-1 b (no refinement), complex128 device."""
+        b = as_c128(b)
+        n = self.op.n
+        nrhs = b.numel() // n
+        x = torch.empty_like(b)
+        N.call("fdfd_factor_solve", self.handle, _ptr(b), _ptr(x), nrhs, int(bool(transpose)), stream_ptr())
+        return x
+
+    def solve(self, b, transpose=False, tol=1e-12, max_iter=10, op: DeviceOperator | None = None,
+              raise_on_fail=False):
+        """x with ||b - A x|| <= tol ||b|| per column (FP64 refinement)."""
+        op = self.op if op is None else op
+        b = as_c128(b)
+        n = op.n
+        nrhs = b.numel() // n
+        x = torch.empty_like(b)
+        s = op.struct()
+        code = N.lib().fdfd_solve_refined(self.handle, C.byref(s), _ptr(b), _ptr(x), nrhs,
+                                          int(bool(transpose)), float(tol), int(max_iter), stream_ptr())
+        if code == N.FDFD_ERR_NOT_CONVERGED and not raise_on_fail:
+            pass
+        else:
+            N.check(code, "fdfd_solve_refined")
+        return x
+
+    def stats(self) -> dict:
+        st = N.FactorStats()
+        N.call("fdfd_factor_stats_get", self.handle, C.byref(st))
+        return {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
+                "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms}
+
+    def __del__(self):
+        try:
+            if self.handle:
+                N.lib().fdfd_factor_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass

@@ -1,0 +1,214 @@
+/*
+ * fdfd_gb300.h -- C ABI of the GB300 (sm_103a) FDFD engine.
+ *
+ * The engine replaces the hot path of fdfdpy: PML-stretched 2D Maxwell
+ * operator assembly (fdfdpy/linalg.py:41-107, fdfdpy/pml.py:7-89,
+ * fdfdpy/derivatives.py:7-34) followed by the complex sparse direct solve
+ * (fdfdpy/linalg.py:122-149) and the field recovery that follows it
+ * (fdfdpy/simulation.py:129-175).
+ *
+ * Conventions shared by every entry point:
+ *   - Plain C types only.  Device buffers are raw pointers owned by the
+ *     caller (any allocator); complex numbers are interleaved (re, im) pairs
+ *     of double (complex128) unless stated otherwise.
+ *   - Grids are (Nx, Ny), C order: unknown k = i*Ny + j, exactly as the
+ *     reference's eps_r.reshape(-1).
+ *   - Every call is ordered on the caller's CUDA stream (`stream`, a
+ *     cudaStream_t passed as void*; NULL = legacy default stream).
+ *   - Every call returns an int status (FDFD_OK = 0) and never throws.
+ *     fdfd_last_error() gives a human-readable message for the calling
+ *     thread.
+ */
+#ifndef FDFD_GB300_H
+#define FDFD_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------- */
+#define FDFD_OK                 0
+#define FDFD_ERR_BAD_ARG        1   /* invalid size, pointer or option      */
+#define FDFD_ERR_OOM            2   /* device allocation refused            */
+#define FDFD_ERR_CUDA           3   /* a CUDA runtime call failed           */
+#define FDFD_ERR_SINGULAR_PIVOT 4   /* a zero pivot was met (not replaced)  */
+#define FDFD_ERR_NOT_CONVERGED  5   /* refinement hit its iteration cap     */
+#define FDFD_ERR_NO_DEVICE      6   /* no CUDA device visible               */
+
+/* ---- polarizations and precisions ------------------------------------- */
+#define FDFD_POL_EZ 0
+#define FDFD_POL_HZ 1
+
+#define FDFD_PREC_C128 0   /* plain: complex128 factor                    */
+#define FDFD_PREC_C64  1   /* mixed: complex64 factor + FP64 refinement   */
+
+/* Operator description.  Mirrors the arguments of construct_A
+ * (fdfdpy/linalg.py:41-44).  All pointers are DEVICE pointers.
+ *   eps      : (Nx*Ny) float64 relative permittivity eps_r.
+ *   eps_add  : optional (Nx*Ny) float64 added to eps_r in the diagonal term
+ *              only (the Kerr term of fdfdpy/simulation.py:57-68); NULL = 0.
+ *   diag_add : optional (Nx*Ny) complex128 added to the operator diagonal
+ *              (Newton Jacobian, fdfdpy/nonlinear_solvers.py:139-141); NULL.
+ *   inv_s    : the four stretched-coordinate factors 1/s as complex128
+ *              vectors: inv_sxf, inv_sxb (Nx each), inv_syf, inv_syb (Ny
+ *              each), from fdfd_pml_sfactors (fdfdpy/pml.py:42-89).
+ *   xlen/ylen: xrange[1]-xrange[0], yrange[1]-yrange[0] (grid spacing is
+ *              xlen/Nx, ylen/Ny as in fdfdpy/linalg.py:25-33).           */
+typedef struct fdfd_operator {
+    int32_t Nx, Ny;
+    int32_t pol;        /* FDFD_POL_EZ or FDFD_POL_HZ                    */
+    int32_t averaging;  /* Hz only: grid-averaged eps (linalg.py:73-78)   */
+    double  omega;
+    double  L0;
+    double  xlen, ylen;
+    const double *eps;
+    const double *eps_add;
+    const void   *diag_add;
+    const void   *inv_sxf, *inv_sxb, *inv_syf, *inv_syb;
+} fdfd_operator;
+
+/* ---- library ----------------------------------------------------------- */
+const char *fdfd_last_error(void);
+int fdfd_version(void);
+
+/* ---- PML ---------------------------------------------------------------
+ * Replaces create_sfactor + the 1/s broadcast of S_create
+ * (fdfdpy/pml.py:7-39, 64-75).  Writes 1/s for one axis:
+ *   out_inv_f, out_inv_b : (Nw) complex128 device vectors.
+ * wlen = wrange[1]-wrange[0].                                            */
+int fdfd_pml_sfactors(int32_t Nw, int32_t Nw_pml, double wlen, double omega,
+                      double L0, void *out_inv_f, void *out_inv_b,
+                      void *stream);
+
+/* ---- K1: operator assembly --------------------------------------------
+ * Replaces construct_A (fdfdpy/linalg.py:41-107).  Emits canonical CSR
+ * (rows sorted by column): indptr (n+1, int32), indices (5n, int32),
+ * data (5n complex128).  Requires Nx >= 3 and Ny >= 3.                    */
+int fdfd_assemble_csr(const fdfd_operator *op, int32_t *indptr,
+                      int32_t *indices, void *data, void *stream);
+
+/* Emits one derivative operator of the reference's `derivs` dict
+ * (fdfdpy/linalg.py:59-62 / 86-89, 100-105) as canonical CSR with 2 nnz
+ * per row: which = 0 Dxf, 1 Dxb, 2 Dyf, 3 Dyb.                            */
+int fdfd_assemble_deriv_csr(const fdfd_operator *op, int32_t which,
+                            int32_t *indptr, int32_t *indices, void *data,
+                            void *stream);
+
+/* ---- K2: matrix-free FP64 residual ------------------------------------
+ * r = b - A x for nrhs right-hand sides stored column after column
+ * (leading dimension n).  Replaces the mat-vec used by the reference's
+ * residual checks and Newton f(E) (fdfdpy/nonlinear_solvers.py:130-132). */
+int fdfd_residual(const fdfd_operator *op, const void *x, const void *b,
+                  void *r, int32_t nrhs, void *stream);
+
+/* y = A x (or A^T x when transpose != 0).                                */
+int fdfd_apply(const fdfd_operator *op, const void *x, void *y,
+               int32_t nrhs, int32_t transpose, void *stream);
+
+/* ---- K8: field recovery ------------------------------------------------
+ * Replaces fdfdpy/simulation.py:129-175.  From the solved primary field X
+ * (Ez or Hz, complex128 n) writes the two secondary fields:
+ *   Ez: f1 = Hx, f2 = Hy;   Hz: f1 = Ex, f2 = Ey.                        */
+int fdfd_fields(const fdfd_operator *op, const void *X, void *f1, void *f2,
+                void *stream);
+
+/* ---- K9: adjoint gradient ----------------------------------------------
+ * dL/d(eps_r) = -omega^2 * eps0 * L0 * Re(lambda * E) (Ez), written to
+ * grad (n float64).  No counterpart in the reference (it has no
+ * derivative w.r.t. eps); derived from fdfdpy/linalg.py:53-54,66.       */
+int fdfd_adjoint_grad_eps(const fdfd_operator *op, const void *lambda_,
+                          const void *E, double *grad, void *stream);
+
+/* ---- reductions --------------------------------------------------------
+ * Column 2-norms of a complex128 (n x ncol) array, written to host array
+ * out_host (ncol doubles); synchronises the stream.                      */
+int fdfd_norms(const void *v, int64_t n, int32_t ncol, double *out_host,
+               void *stream);
+
+/* ---- symbolic analysis (host only) ------------------------------------
+ * Geometric nested dissection of the periodic Nx x Ny grid (the graph of
+ * construct_A's 5-point operator) into a front tree.  Replaces the fill-
+ * reducing ordering inside PARDISO/SuperLU (fdfdpy/linalg.py:134-141).  */
+typedef struct fdfd_symbolic fdfd_symbolic;
+
+typedef struct fdfd_symbolic_info {
+    int32_t Nx, Ny;
+    int32_t n_fronts;
+    int32_t n_levels;
+    int64_t sum_m;          /* total front index-list length             */
+    int64_t pool_entries;   /* sum over fronts of ld*m                   */
+    int64_t factor_entries; /* sum p^2 + 2 p (m-p): stored L+U entries   */
+    double  factor_flops;   /* real flops of the complex partial LUs     */
+    int32_t max_m, max_p;
+} fdfd_symbolic_info;
+
+int fdfd_symbolic_create(int32_t Nx, int32_t Ny, int32_t leaf_area,
+                         fdfd_symbolic **out);
+int fdfd_symbolic_info_get(const fdfd_symbolic *sym, fdfd_symbolic_info *info);
+/* Copies one host array out (tests and diagnostics).  which:
+ *  0 front p (n_fronts int32)     1 front m          2 front parent
+ *  3 front child0                 4 front child1     5 front height
+ *  6 front vars_off (int32)       7 level_ptr (n_levels+1 int32)
+ *  8 vars (sum_m int32)           9 relmap (sum_m int32)
+ * 10 nbr_loc (4n int32)          11 var_front (n)   12 var_loc (n)
+ * 13 front ld (int32)            14 pool_off (n_fronts int64)           */
+int fdfd_symbolic_export(const fdfd_symbolic *sym, int32_t which, void *dst);
+void fdfd_symbolic_destroy(fdfd_symbolic *sym);
+
+/* ---- numeric factorization ---------------------------------------------
+ * Multifrontal LU of the operator over the symbolic front tree, without
+ * pivoting (static pivots; tiny pivots are replaced and counted).
+ * Replaces pardisoSolver(A, mtype=13).factor() (fdfdpy/linalg.py:135-136)
+ * and the factor inside spsolve (linalg.py:141).  The factor owns its
+ * device memory (allocated on the current device at create time).        */
+typedef struct fdfd_factor fdfd_factor;
+
+typedef struct fdfd_factor_stats {
+    int32_t tiny_pivots;    /* pivots replaced by the static threshold   */
+    int32_t refine_iters;   /* refinement steps of the last solve        */
+    double  rel_residual;   /* ||b - A x|| / ||b|| of the last solve (max */
+                            /* over right-hand sides)                     */
+    double  factor_ms;      /* device time of the last factorization     */
+    double  solve_ms;       /* device time of the last solve             */
+} fdfd_factor_stats;
+
+int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision,
+                      int32_t max_nrhs, int64_t *bytes);
+int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision,
+                       int32_t max_nrhs, fdfd_factor **out);
+int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op,
+                        void *stream);
+/* One application of the factor: x = A^-1 b (transpose = 0) or
+ * x = A^-T b (transpose = 1), complex128 in and out, nrhs columns.       */
+int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x,
+                      int32_t nrhs, int32_t transpose, void *stream);
+/* Solve with FP64 iterative refinement against the matrix-free operator
+ * until max_j ||b_j - A x_j|| / ||b_j|| <= tol or max_iter steps.
+ * Replaces solver_direct (fdfdpy/linalg.py:122-149).  Returns
+ * FDFD_ERR_NOT_CONVERGED (x still written) when tol was not reached.    */
+int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
+                       const void *b, void *x, int32_t nrhs,
+                       int32_t transpose, double tol, int32_t max_iter,
+                       void *stream);
+int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st);
+void fdfd_factor_destroy(fdfd_factor *fac);
+
+/* ---- profiling -----------------------------------------------------------
+ * Launch counters per kernel class are always kept; CUDA-event timing of
+ * each class is recorded while enabled.  Classes: 0 front assembly,
+ * 1 extend-add, 2 diagonal-block LU, 3 panel TRSM, 4 Schur GEMM,
+ * 5 forward solve, 6 backward solve, 7 residual / norms / scaling.
+ * Replaces the `timing=` prints of the reference (fdfdpy/linalg.py:131-147).
+ * Not thread-safe: profile one stream at a time.                         */
+int fdfd_profile_enable(int32_t on);
+int fdfd_profile_reset(void);
+/* Synchronises on the recorded events; writes nclass (<= 8) entries.     */
+int fdfd_profile_read(int32_t nclass, double *ms, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDFD_GB300_H */

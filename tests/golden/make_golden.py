@@ -1,0 +1,188 @@
+"""Generate golden vectors by running the reference fdfdpy itself.
+
+Run in a container that has the reference checkout (default
+/root/reference, or $FDFDPY_REFERENCE):
+
+    python tests/golden/make_golden.py
+
+The reference imports pyMKL (absent here) and matplotlib (absent); both are
+replaced by sys.modules shims before import:
+  * pyMKL.pardisoSolver -> an exact SuperLU factor (scipy splu), so the
+    reference's default solver='pardiso' path runs through SuperLU;
+  * matplotlib          -> an empty module (plotting is not exercised).
+The reference's Hz branch calls an unimported ``eye`` (fdfdpy/linalg.py:93);
+the shim sets ``fdfdpy.linalg.eye = scipy.sparse.eye`` (its evident intent).
+
+Outputs (small .npz files beside this script) hold inputs and outputs of
+sfactor/construct_A/derivs/solve_fields/mode sources at sizes that take
+seconds.  Nothing at test time reads the reference.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spl
+
+OUT = Path(__file__).resolve().parent
+REF = os.environ.get("FDFDPY_REFERENCE", "/root/reference")
+
+
+def install_shims():
+    pm = types.ModuleType("pyMKL")
+
+    class pardisoSolver:  # exact LU stand-in for MKL PARDISO
+        def __init__(self, A, mtype):
+            self.A = sp.csc_matrix(A)
+
+        def factor(self):
+            self.lu = spl.splu(self.A)
+
+        def solve(self, b):
+            return self.lu.solve(np.asarray(b))
+
+        def clear(self):
+            pass
+
+    pm.pardisoSolver = pardisoSolver
+    sys.modules["pyMKL"] = pm
+    mpl = types.ModuleType("matplotlib")
+    mpl.pyplot = types.ModuleType("matplotlib.pyplot")
+    mpl.pylab = mpl.pyplot
+    sys.modules["matplotlib"] = mpl
+    sys.modules["matplotlib.pyplot"] = mpl.pyplot
+    sys.modules["matplotlib.pylab"] = mpl.pyplot
+    sys.path.insert(0, REF)
+    import fdfdpy.linalg as L
+    L.eye = sp.eye
+
+
+def canon(A):
+    A = sp.csr_matrix(A, copy=True)
+    A.sort_indices()
+    return A
+
+
+def main():
+    install_shims()
+    import warnings
+    warnings.simplefilter("ignore")
+    from fdfdpy import Simulation
+    from fdfdpy.constants import C_0
+    from fdfdpy.linalg import construct_A
+    from fdfdpy.pml import create_sfactor
+
+    omega155 = 2 * np.pi * C_0 / 1.55e-6
+
+    # 1. stretch factors
+    sf = {}
+    for tag, (wlen, Nw, npml, om, L0) in {
+        "a": (4.0, 200, 15, omega155, 1e-6),
+        "b": (20.48, 2048, 20, omega155, 1e-6),
+        "c": (3.4, 17, 4, 2 * np.pi * 200e12, 1e-6),
+        "d": (0.05, 50, 10, 100.0, 1e-4),
+        "e": (1.0, 10, 0, omega155, 1e-6),
+    }.items():
+        sf[f"{tag}_args"] = np.array([wlen, Nw, npml, om, L0])
+        sf[f"{tag}_f"] = create_sfactor([0, wlen], L0, "f", om, Nw, npml)
+        sf[f"{tag}_b"] = create_sfactor([0, wlen], L0, "b", om, Nw, npml)
+    np.savez_compressed(OUT / "sfactors.npz", **sf)
+
+    # 2. small operators, derivatives and solved fields (all three solvers
+    #    paths agree: scipy spsolve and the pardiso stand-in)
+    rng = np.random.default_rng(1234)
+    cases = {
+        "ez_24x17": (24, 17, [5, 4], "Ez", 0.02, omega155, 1e-6),
+        "hz_24x17": (24, 17, [5, 4], "Hz", 0.02, omega155, 1e-6),
+        "ez_40x40": (40, 40, [10, 10], "Ez", 0.02, omega155, 1e-6),
+        "hz_33x20_npml0": (33, 20, [0, 3], "Hz", 0.05, 2 * np.pi * 200e12, 1e-6),
+        "ez_12x9_L0": (12, 9, [2, 2], "Ez", 0.001, 100.0, 1e-4),
+    }
+    small = {}
+    for name, (Nx, Ny, npml, pol, dl, om, L0) in cases.items():
+        eps = 1 + 11 * rng.random((Nx, Ny))
+        sim = Simulation(om, eps, dl, npml, pol, L0=L0)
+        A = canon(sim.A)
+        small[f"{name}_args"] = np.array([Nx, Ny, npml[0], npml[1], dl, om, L0, 0 if pol == "Ez" else 1])
+        small[f"{name}_eps"] = eps
+        small[f"{name}_indptr"] = A.indptr
+        small[f"{name}_indices"] = A.indices
+        small[f"{name}_data"] = A.data
+        for dn, D in sim.derivs.items():
+            small[f"{name}_{dn}"] = canon(D).data
+        src = np.zeros((Nx, Ny))
+        src[Nx // 2, Ny // 3] = 1.0
+        src[Nx // 3, Ny // 2] = -0.5
+        sim.src = src
+        f = sim.solve_fields(solver="scipy")
+        small[f"{name}_src"] = src
+        for fi, fv in zip(("f1", "f2", "f3"), f):
+            small[f"{name}_{fi}"] = fv
+        if pol == "Hz":
+            A2, _ = construct_A(om, sim.xrange, sim.yrange, eps, npml, pol, L0, averaging=False)
+            small[f"{name}_noavg_data"] = canon(A2).data
+            f = sim.solve_fields(solver="scipy", averaging=False)
+            small[f"{name}_noavg_f1"] = f[0]
+            small[f"{name}_noavg_f2"] = f[1]
+    np.savez_compressed(OUT / "small_ops.npz", **small)
+
+    # 3. the 200x200 Ez point-source problem (eps 12 square)
+    N = 200
+    eps = np.ones((N, N))
+    eps[80:120, 80:120] = 12
+    sim = Simulation(omega155, eps, 0.02, [15, 15], "Ez")
+    sim.src[100, 100] = 1
+    A = canon(sim.A)
+    Hx, Hy, Ez = sim.solve_fields(solver="scipy")
+    rows = np.arange(0, N * N, 37)
+    g = {
+        "rows": rows,
+        "row_indices": np.stack([A.indices[A.indptr[r]:A.indptr[r + 1]] for r in rows]),
+        "row_data": np.stack([A.data[A.indptr[r]:A.indptr[r + 1]] for r in rows]),
+        "data_abs_sum": np.abs(A.data).sum(),
+        "sample": np.arange(0, N * N, 5),
+        "Hx": Hx.reshape(-1)[::5], "Hy": Hy.reshape(-1)[::5], "Ez": Ez.reshape(-1)[::5],
+        "norms": np.array([np.linalg.norm(Hx), np.linalg.norm(Hy), np.linalg.norm(Ez)]),
+        "relres": np.linalg.norm(sim.A @ Ez.reshape(-1) - 1j * omega155 * sim.src.reshape(-1))
+        / np.linalg.norm(1j * omega155 * sim.src.reshape(-1)),
+    }
+    np.savez_compressed(OUT / "ez200.npz", **g)
+
+    # 4. Hz piecewise-constant blocks (the 2048^2 workload's family at 128^2)
+    N = 128
+    r0 = np.random.default_rng(0)
+    eps = np.kron(r0.choice([1.0, 12.25], size=(N // 16, N // 16)), np.ones((16, 16)))
+    sim = Simulation(omega155, eps, 0.01, [20, 20], "Hz")
+    sim.src[30, :] = 1
+    Ex, Ey, Hz = sim.solve_fields(solver="scipy")
+    np.savez_compressed(OUT / "hz128_blocks.npz", eps=eps, Ex=Ex, Ey=Ey, Hz=Hz)
+
+    # 5. mode source: the ridge waveguide of the examples notebook (Ez) and
+    #    an Hz variant; W_in, E2_in and the inserted source line
+    md = {}
+    for pol in ("Ez", "Hz"):
+        om = 2 * np.pi * 200e12
+        eps = np.ones((600, 200))
+        eps[:, 90:110] = 12.25
+        sim = Simulation(om, eps, 0.01, [15, 15], pol)
+        sim.add_mode(3.5, "x", [20, 100], 60, scale=10)
+        if pol == "Ez":
+            sim.setup_modes()
+            md["ez_W_in"] = sim.W_in
+            md["ez_E2_in"] = sim.E2_in
+        else:
+            # E2_in reads fields['Ez'] (mode.py:59-60), which the Hz branch
+            # never fills, so only the source insertion is recorded for Hz.
+            sim.modes[0].insert_mode(sim, sim.src)
+        md[f"{pol.lower()}_src_line"] = sim.src[20, 70:130].copy()
+    np.savez_compressed(OUT / "modes.npz", **md)
+
+    print("golden vectors written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

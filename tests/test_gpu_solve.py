@@ -1,0 +1,138 @@
+"""GPU multifrontal factor + solve against the oracle (SuperLU) and the
+golden fields of the reference.
+
+Bars (fields, relative 2-norm): complex128 factor <= 1e-10; complex64
+factor + FP64 refinement to a residual of 1e-10 <= 1e-8 (field error is
+bounded by cond(A) x residual; the refined residual itself is checked
+<= 1e-10).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import fdfd_oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+OMEGA = 2 * np.pi * O.C_0 / 1.55e-6
+
+
+@pytest.fixture(scope="module")
+def eng():
+    from fdfdpy_gb300 import engine
+    engine.device()
+    return engine
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def _problem(Nx, Ny, pol, seed=0, npml=(6, 5), dl=0.02):
+    rng = np.random.default_rng(seed)
+    eps = 1 + 11 * rng.random((Nx, Ny))
+    A = O.construct_A(OMEGA, Nx * dl, Ny * dl, eps, list(npml), pol, 1e-6)
+    return eps, A, rng
+
+
+@pytest.mark.parametrize("Nx,Ny,pol,leaf", [(3, 3, "Ez", 1), (8, 8, "Ez", 4), (17, 13, "Hz", 16),
+                                            (64, 48, "Ez", 64), (97, 131, "Hz", 64), (150, 7, "Ez", 16)])
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_solve_matches_superlu(eng, Nx, Ny, pol, leaf, prec):
+    npml = (min(6, Nx // 3), min(5, Ny // 3))
+    eps, A, rng = _problem(Nx, Ny, pol, npml=npml)
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, list(npml), pol, 1e-6)
+    fac = eng.Factor(eng.Symbolic(Nx, Ny, leaf), prec, max_nrhs=3).numeric(op)
+    b = rng.standard_normal((3, Nx * Ny)) + 1j * rng.standard_normal((3, Nx * Ny))
+    x = fac.solve(b, tol=1e-12 if prec == "c128" else 1e-10, max_iter=40, raise_on_fail=True)
+    x = x.cpu().numpy()
+    st = fac.stats()
+    assert st["rel_residual"] <= (1e-12 if prec == "c128" else 1e-10)
+    for k in range(3):
+        xr = O.solve(A, b[k])
+        assert rel(x[k], xr) < (1e-10 if prec == "c128" else 1e-8), (k, st)
+        assert np.linalg.norm(A @ x[k] - b[k]) / np.linalg.norm(b[k]) < 1e-10
+
+
+def test_single_application_and_transpose(eng):
+    Nx, Ny = 40, 36
+    eps, A, rng = _problem(Nx, Ny, "Ez", seed=2)
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Ez", 1e-6)
+    fac = eng.Factor(eng.Symbolic(Nx, Ny), "c128").numeric(op)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    x1 = fac.apply_inverse(b).cpu().numpy()
+    assert rel(x1, O.solve(A, b)) < 1e-10
+    xt = fac.apply_inverse(b, transpose=True).cpu().numpy()
+    assert rel(xt, O.solve(A.T.tocsr(), b)) < 1e-10
+    xt2 = fac.solve(b, transpose=True, tol=1e-13, max_iter=5).cpu().numpy()
+    assert np.linalg.norm(A.T @ xt2 - b) / np.linalg.norm(b) < 1e-12
+
+
+def test_factor_is_deterministic(eng):
+    Nx, Ny = 70, 70
+    eps, A, rng = _problem(Nx, Ny, "Hz", seed=4)
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Hz", 1e-6)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    sym = eng.Symbolic(Nx, Ny)
+    xs = []
+    for _ in range(2):
+        fac = eng.Factor(sym, "c64").numeric(op)
+        xs.append(fac.apply_inverse(b).cpu().numpy())
+    assert np.array_equal(xs[0], xs[1])
+
+
+def test_ez200_matches_reference_fields(eng):
+    from fdfdpy_gb300 import Simulation
+    g = np.load(GOLD / "ez200.npz")
+    N = 200
+    eps = np.ones((N, N))
+    eps[80:120, 80:120] = 12
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-8)):
+        sim = Simulation(OMEGA, eps, 0.02, [15, 15], "Ez")
+        sim.src[100, 100] = 1
+        Hx, Hy, Ez = sim.solve_fields(precision=prec)
+        s = g["sample"]
+        for got, key in ((Hx, "Hx"), (Hy, "Hy"), (Ez, "Ez")):
+            assert rel(got.reshape(-1)[s], g[key]) < tol, (prec, key)
+        norms = [np.linalg.norm(Hx), np.linalg.norm(Hy), np.linalg.norm(Ez)]
+        assert np.allclose(norms, g["norms"], rtol=tol)
+        assert sim.last_solve_stats["rel_residual"] <= (1e-12 if prec == "c128" else 1e-10)
+
+
+def test_hz_blocks_matches_reference_fields(eng):
+    from fdfdpy_gb300 import Simulation
+    g = np.load(GOLD / "hz128_blocks.npz")
+    sim = Simulation(OMEGA, g["eps"], 0.01, [20, 20], "Hz")
+    sim.src[30, :] = 1
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-8)):
+        Ex, Ey, Hz = sim.solve_fields(precision=prec)
+        assert rel(Hz, g["Hz"]) < tol and rel(Ex, g["Ex"]) < tol and rel(Ey, g["Ey"]) < tol
+
+
+def test_zero_source_and_factor_reuse(eng):
+    from fdfdpy_gb300 import Simulation
+    eps = np.ones((30, 30))
+    sim = Simulation(OMEGA, eps, 0.02, [5, 5], "Ez")
+    Hx, Hy, Ez = sim.solve_fields()
+    assert Ez.dtype == np.float64 and not Ez.any() and not Hx.any()
+    sim.src[15, 15] = 1
+    sim.solve_fields()
+    fac = next(iter(sim._factors.values()))
+    sim.src[10, 12] = 2
+    sim.solve_fields()
+    assert next(iter(sim._factors.values())) is fac  # only the source changed
+    sim.eps_r = eps * 2
+    assert sim.fields["Ez"] is None and not sim._factors
+
+
+def test_not_converged_is_reported(eng):
+    from fdfdpy_gb300 import _native as N
+    Nx, Ny = 60, 60
+    eps, A, rng = _problem(Nx, Ny, "Ez", seed=9)
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Ez", 1e-6)
+    fac = eng.Factor(eng.Symbolic(Nx, Ny), "c64").numeric(op)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    with pytest.raises(N.NotConverged):
+        fac.solve(b, tol=1e-15, max_iter=0, raise_on_fail=True)
