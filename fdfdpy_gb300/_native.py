@@ -39,7 +39,7 @@ class Operator(C.Structure):
         ("omega", C.c_double), ("L0", C.c_double), ("xlen", C.c_double), ("ylen", C.c_double),
         ("eps", C.c_void_p), ("eps_add", C.c_void_p), ("diag_add", C.c_void_p),
         ("inv_sxf", C.c_void_p), ("inv_sxb", C.c_void_p), ("inv_syf", C.c_void_p),
-        ("inv_syb", C.c_void_p),
+        ("inv_syb", C.c_void_p), ("stencil", C.c_void_p),
     ]
 
 
@@ -75,6 +75,7 @@ SIGNATURES = {
     "fdfd_apply": (C.c_int, [POP, P, P, I32, I32, P]),
     "fdfd_fields": (C.c_int, [POP, P, P, P, P]),
     "fdfd_adjoint_grad_eps": (C.c_int, [POP, P, P, P, P]),
+    "fdfd_mode_stencil": (C.c_int, [I32, I32, I32, P, D, D, D, D, P, P]),
     "fdfd_norms": (C.c_int, [P, I64, I32, P, P]),
     "fdfd_symbolic_create": (C.c_int, [I32, I32, I32, C.POINTER(P)]),
     "fdfd_symbolic_info_get": (C.c_int, [P, C.POINTER(SymbolicInfo)]),

@@ -100,18 +100,21 @@ __global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
         const int k = var_loc[s];
         double2 c[5];
         stencil_row(o, i, j, c);
-        F[k + k * ld] = from_c128<T>(c[0], sigma);
+        // Each (row, column) of a front is written by one thread only; the
+        // += sums couplings to neighbours that coincide (grids thinner
+        // than 3 cells, explicit-stencil operators).
+        F[k + k * ld] = cadd(F[k + k * ld], from_c128<T>(c[0], sigma));
         for (int d = 0; d < 4; ++d) {
             const int nl = nbr_loc[4 * s + d];
             if (nl < 0) continue;
-            F[k + nl * ld] = from_c128<T>(c[1 + d], sigma);
+            F[k + nl * ld] = cadd(F[k + nl * ld], from_c128<T>(c[1 + d], sigma));
             if (nl >= f.p) {
                 // A[t, s] for the boundary neighbour t: t's coefficient
                 // pointing back towards s.
                 const int t = nbr_cell(o, i, j, d);
                 double2 ct[5];
                 stencil_row(o, t / o.Ny, t % o.Ny, ct);
-                F[nl + k * ld] = from_c128<T>(ct[1 + opposite_dir(d)], sigma);
+                F[nl + k * ld] = cadd(F[nl + k * ld], from_c128<T>(ct[1 + opposite_dir(d)], sigma));
             }
         }
     }
@@ -552,6 +555,7 @@ struct fdfd_factor {
     double *h_norm = nullptr;  // pinned
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool numeric_done = false;
+    bool has_p = false;  // PML factors known: transposed solves allowed
     int Nx = 0, Ny = 0;
     fdfd_factor_stats stats{};
 };
@@ -684,6 +688,8 @@ __global__ void k_colscale(const double2 *in, double2 *out, const double *s, int
 int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, int transpose,
                  cudaStream_t st) {
     const int64_t n = fac->n;
+    if (transpose && !fac->has_p)
+        return fail(FDFD_ERR_BAD_ARG, "transposed solve needs the operator's PML factors");
     double2 *tmp = fac->d_tmp;
     const double2 *src = in;
     if (transpose) {
@@ -760,7 +766,7 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         return fail(FDFD_ERR_BAD_ARG, "factor_create: unknown precision");
     if (max_nrhs < 1 || max_nrhs > 8) return fail(FDFD_ERR_BAD_ARG, "factor_create: max_nrhs must be 1..8");
     const Symbolic &S = sym->s;
-    if (S.Nx < 3 || S.Ny < 3) return fail(FDFD_ERR_BAD_ARG, "factor_create: grid must be at least 3x3");
+
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -844,8 +850,11 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
     if (op->Nx != fac->Nx || op->Ny != fac->Ny)
         return fail(FDFD_ERR_BAD_ARG, "factor_numeric: operator grid differs from the symbolic grid");
     cudaStream_t st = (cudaStream_t)stream;
-    CUDA_TRY(cudaMemcpyAsync(fac->d_isxf, op->inv_sxf, fac->Nx * 16, cudaMemcpyDeviceToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(fac->d_isyf, op->inv_syf, fac->Ny * 16, cudaMemcpyDeviceToDevice, st));
+    fac->has_p = op->inv_sxf && op->inv_syf;
+    if (fac->has_p) {
+        CUDA_TRY(cudaMemcpyAsync(fac->d_isxf, op->inv_sxf, fac->Nx * 16, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(fac->d_isyf, op->inv_syf, fac->Ny * 16, cudaMemcpyDeviceToDevice, st));
+    }
     CUDA_TRY(cudaEventRecord(fac->ev[0], st));
     rc = (fac->precision == FDFD_PREC_C64) ? factor_levels<c64, float>(fac, o, st)
                                            : factor_levels<c128, double>(fac, o, st);

@@ -231,6 +231,40 @@ __global__ void k_fields(OpDev o, const double2 *__restrict__ X, double2 *__rest
     }
 }
 
+// ---- mode-source slice operator (fdfdpy/source/mode.py:76-91) ------------
+__global__ void k_mode_stencil(int N, int pol, int average, const double *eps, double w2mu0,
+                               double eps0L, double v, double shift, double2 *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const int im = (i == 0) ? N - 1 : i - 1, ip = (i == N - 1) ? 0 : i + 1;
+        const double e = __dmul_rn(eps0L, eps[i]);
+        double c, xm, xp;
+        // Dxf Dxb rows: (-v)(v e_i - v e_{i-1}) + v (v e_{i+1} - v e_i)
+        const double vv = __dmul_rn(v, v);
+        if (pol == FDFD_POL_EZ) {
+            xm = vv;
+            xp = vv;
+            c = __dadd_rn(__dmul_rn(w2mu0, e), __dsub_rn(-vv, vv));
+        } else {
+            // eps_x = eps0' * grid_average(eps): averaged along the slice
+            // only when the slice runs along the rolled axis
+            const double ax0 = average ? __dmul_rn(__dadd_rn(eps[im], eps[i]), 0.5) : eps[i];
+            const double ax1 = average ? __dmul_rn(__dadd_rn(eps[i], eps[ip]), 0.5) : eps[ip];
+            const double t0 = __ddiv_rn(1.0, __dmul_rn(eps0L, ax0));
+            const double t1 = __ddiv_rn(1.0, __dmul_rn(eps0L, ax1));
+            // ((T_eps Dxf) T_epsx^-1) Dxb, evaluated left to right
+            const double ev = __dmul_rn(e, v);
+            xm = __dmul_rn(__dmul_rn(ev, t0), v);
+            xp = __dmul_rn(__dmul_rn(ev, t1), v);
+            c = __dadd_rn(__dmul_rn(w2mu0, e), -__dadd_rn(xm, xp));
+        }
+        out[i] = make_double2(c - shift, 0.0);
+        out[N + i] = make_double2(xm, 0.0);
+        out[2 * N + i] = make_double2(xp, 0.0);
+        out[3 * N + i] = make_double2(0.0, 0.0);
+        out[4 * N + i] = make_double2(0.0, 0.0);
+    }
+}
+
 // ---- K9: adjoint gradient ------------------------------------------------
 __global__ void k_grad_eps(int64_t n, double coef, const double2 *__restrict__ lam,
                            const double2 *__restrict__ E, double *__restrict__ g) {
@@ -305,16 +339,28 @@ int apply_device(const OpDev &o, const void *x, const void *b, void *out, int nr
 
 int make_opdev(const fdfd_operator *op, OpDev *d) {
     if (!op) return fail(FDFD_ERR_BAD_ARG, "operator is NULL");
-    if (op->Nx < 3 || op->Ny < 3)
+    if (op->stencil) {
+        if (op->Nx < 1 || op->Ny < 1) return fail(FDFD_ERR_BAD_ARG, "operator: empty grid");
+    } else if (op->Nx < 3 || op->Ny < 3) {
         return fail(FDFD_ERR_BAD_ARG, "operator: the GPU operator needs Nx >= 3 and Ny >= 3");
+    }
     if ((int64_t)op->Nx * op->Ny > ((int64_t)1 << 30) / 5)
         return fail(FDFD_ERR_BAD_ARG, "operator: grid too large for int32 CSR indices");
     if (op->pol != FDFD_POL_EZ && op->pol != FDFD_POL_HZ)
         return fail(FDFD_ERR_BAD_ARG, "operator: pol must be FDFD_POL_EZ or FDFD_POL_HZ");
-    if (!op->eps || !op->inv_sxf || !op->inv_sxb || !op->inv_syf || !op->inv_syb)
+    if (!op->stencil && (!op->eps || !op->inv_sxf || !op->inv_sxb || !op->inv_syf || !op->inv_syb))
         return fail(FDFD_ERR_BAD_ARG, "operator: eps and the four 1/s vectors are required");
-    if (!(op->xlen > 0.0) || !(op->ylen > 0.0) || !(op->L0 > 0.0))
+    if (!op->stencil && (!(op->xlen > 0.0) || !(op->ylen > 0.0) || !(op->L0 > 0.0)))
         return fail(FDFD_ERR_BAD_ARG, "operator: xlen, ylen and L0 must be positive");
+    d->stencil = (const double2 *)op->stencil;
+    if (op->stencil) {
+        d->Nx = op->Nx; d->Ny = op->Ny; d->pol = op->pol; d->averaging = 0;
+        d->invdx = d->invdy = d->invmu = d->eps0L = d->w2 = d->w2mu = d->w2e0L = 0.0;
+        d->eps = nullptr; d->eps_add = nullptr; d->diag_add = nullptr;
+        d->isxf = (const double2 *)op->inv_sxf; d->isxb = (const double2 *)op->inv_sxb;
+        d->isyf = (const double2 *)op->inv_syf; d->isyb = (const double2 *)op->inv_syb;
+        return FDFD_OK;
+    }
     d->Nx = op->Nx; d->Ny = op->Ny; d->pol = op->pol; d->averaging = op->averaging ? 1 : 0;
     const double dx = op->xlen / op->Nx, dy = op->ylen / op->Ny;  // linalg.py:25-33
     d->invdx = 1.0 / dx;
@@ -366,6 +412,7 @@ extern "C" int fdfd_assemble_csr(const fdfd_operator *op, int32_t *indptr, int32
     OpDev o;
     int st = make_opdev(op, &o);
     if (st) return st;
+    if (o.stencil) return fail(FDFD_ERR_BAD_ARG, "assemble_csr: needs the physical operator, not a stencil");
     if (!indptr || !indices || !data) return fail(FDFD_ERR_BAD_ARG, "assemble_csr: NULL output");
     const int64_t n = (int64_t)o.Nx * o.Ny;
     k_assemble_csr<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(o, indptr, indices,
@@ -378,6 +425,7 @@ extern "C" int fdfd_assemble_deriv_csr(const fdfd_operator *op, int32_t which, i
     OpDev o;
     int st = make_opdev(op, &o);
     if (st) return st;
+    if (o.stencil) return fail(FDFD_ERR_BAD_ARG, "assemble_deriv_csr: needs the physical operator, not a stencil");
     if (which < 0 || which > 3) return fail(FDFD_ERR_BAD_ARG, "assemble_deriv_csr: which must be 0..3");
     if (!indptr || !indices || !data) return fail(FDFD_ERR_BAD_ARG, "assemble_deriv_csr: NULL output");
     const int64_t n = (int64_t)o.Nx * o.Ny;
@@ -408,6 +456,7 @@ extern "C" int fdfd_fields(const fdfd_operator *op, const void *X, void *f1, voi
     OpDev o;
     int st = make_opdev(op, &o);
     if (st) return st;
+    if (o.stencil) return fail(FDFD_ERR_BAD_ARG, "fields: needs the physical operator, not a stencil");
     if (!X || !f1 || !f2) return fail(FDFD_ERR_BAD_ARG, "fields: NULL buffer");
     // Scalars of fdfdpy/simulation.py:148-149 (Hz) and 163-164 (Ez), as
     // Python evaluates them: -1/1j = 1j, 1/1j = -1j, then divisions by
@@ -433,6 +482,7 @@ extern "C" int fdfd_adjoint_grad_eps(const fdfd_operator *op, const void *lambda
     OpDev o;
     int st = make_opdev(op, &o);
     if (st) return st;
+    if (o.stencil) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: needs the physical operator, not a stencil");
     if (!lambda_ || !E || !grad) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: NULL buffer");
     if (o.pol != FDFD_POL_EZ) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: only Ez is supported");
     const int64_t n = (int64_t)o.Nx * o.Ny;
@@ -457,4 +507,18 @@ extern "C" int fdfd_norms(const void *v, int64_t n, int32_t ncol, double *out_ho
     }
     cudaFreeAsync(buf, st);
     return rc;
+}
+
+extern "C" int fdfd_mode_stencil(int32_t N, int32_t pol, int32_t average, const double *eps_slice,
+                                 double omega, double dl, double L0, double shift, void *out,
+                                 void *stream) {
+    if (N < 1 || !eps_slice || !out) return fail(FDFD_ERR_BAD_ARG, "mode_stencil: bad size or NULL buffer");
+    if (pol != FDFD_POL_EZ && pol != FDFD_POL_HZ) return fail(FDFD_ERR_BAD_ARG, "mode_stencil: bad pol");
+    if (!(dl > 0.0) || !(L0 > 0.0)) return fail(FDFD_ERR_BAD_ARG, "mode_stencil: dl and L0 must be positive");
+    const double w2mu0 = (omega * omega) * (MU_0 * L0);  // np.square(omega)*MU_0_
+    const double v = 1.0 / dl;
+    k_mode_stencil<<<grid_for(N), kThreads, 0, (cudaStream_t)stream>>>(N, pol, average, eps_slice, w2mu0,
+                                                                      EPSILON_0 * L0, v, shift,
+                                                                      (double2 *)out);
+    return launch_status("mode_stencil");
 }

@@ -31,6 +31,7 @@ struct OpDev {
     const double *eps_add;
     const double2 *diag_add;
     const double2 *isxf, *isxb, *isyf, *isyb;
+    const double2 *stencil;  // explicit coefficients [5][n], or NULL
 };
 
 // Validates a public operator description and derives the device scalars.
@@ -73,6 +74,12 @@ __device__ __forceinline__ double inv_eps_y(const OpDev &o, int i, int j) {
 // c[4] (i, j+1), all complex128.
 __device__ inline void stencil_row(const OpDev &o, int i, int j, double2 c[5]) {
     const int Nx = o.Nx, Ny = o.Ny;
+    if (o.stencil) {
+        const size_t n = (size_t)Nx * Ny, k = (size_t)i * Ny + j;
+#pragma unroll
+        for (int d = 0; d < 5; ++d) c[d] = o.stencil[d * n + k];
+        return;
+    }
     const int ip = (i == Nx - 1) ? 0 : i + 1;
     const int jp = (j == Ny - 1) ? 0 : j + 1;
     const size_t k = (size_t)i * Ny + j;

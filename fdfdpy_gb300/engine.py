@@ -294,3 +294,77 @@ class Factor:
                 self.handle = None
         except Exception:
             pass
+
+
+class StencilOperator:
+    """An explicit periodic 5-point operator on an Nx x Ny grid (complex128
+    coefficients [5][n] on the device); factored by the same engine."""
+
+    def __init__(self, Nx, Ny, stencil: torch.Tensor, pol="Ez"):
+        self.Nx, self.Ny, self.pol = int(Nx), int(Ny), pol
+        self.stencil = stencil.reshape(5, -1).contiguous()
+        assert self.stencil.dtype == torch.complex128 and self.stencil.shape[1] == self.Nx * self.Ny
+
+    @property
+    def n(self):
+        return self.Nx * self.Ny
+
+    def struct(self, **_):
+        op = N.Operator()
+        op.Nx, op.Ny, op.pol, op.averaging = self.Nx, self.Ny, N.POL[self.pol], 0
+        op.omega, op.L0, op.xlen, op.ylen = 1.0, 1.0, 1.0, 1.0
+        op.stencil = self.stencil.data_ptr()
+        return op
+
+    def apply(self, x, transpose=False):
+        x = as_c128(x)
+        y = torch.empty_like(x)
+        op = self.struct()
+        N.call("fdfd_apply", C.byref(op), _ptr(x), _ptr(y), x.numel() // self.n, int(bool(transpose)),
+               stream_ptr())
+        return y
+
+    @staticmethod
+    def mode_slice(pol, eps_slice, omega, dl, L0, shift, average):
+        """Slice operator of insert_mode minus shift * I (N x 1 grid)."""
+        e = as_f64(eps_slice).reshape(-1)
+        Ns = e.numel()
+        st = torch.empty(5 * Ns, dtype=torch.complex128, device=e.device)
+        N.call("fdfd_mode_stencil", Ns, N.POL[pol], int(bool(average)), _ptr(e), float(omega), float(dl),
+               float(L0), float(shift), _ptr(st), stream_ptr())
+        return StencilOperator(Ns, 1, st, pol)
+
+
+def shift_invert_eigs(op_shifted: StencilOperator, shift: float, k: int, tol=1e-12, max_iter=500,
+                      seed=0):
+    """The k eigenpairs of A nearest `shift`, from the factor of A - shift I
+    (shift-invert block subspace iteration + Rayleigh-Ritz).  Returns
+    (values, vectors (n, k)) ordered by distance to the shift, vectors of
+    unit 2-norm.  Replaces ARPACK's eigs(A, k, sigma=shift, which='LM')
+    (fdfdpy/linalg.py:110-119)."""
+    n = op_shifted.n
+    kb = int(min(n, max(k + 2, 2), 8))
+    fac = Factor(symbolic_for(op_shifted.Nx, op_shifted.Ny, 1), "c128", max_nrhs=kb).numeric(op_shifted)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    V = torch.randn(n, kb, generator=g, dtype=torch.float64).to(torch.complex128).to(device())
+    V, _ = torch.linalg.qr(V)
+    lam = vecs = None
+    for _ in range(max_iter):
+        W = fac.apply_inverse(V.T.contiguous()).reshape(kb, n).T
+        V, _ = torch.linalg.qr(W)
+        AV = op_shifted.apply(V.T.contiguous()).reshape(kb, n).T
+        H = (V.conj().T @ AV).cpu()
+        mu, S = torch.linalg.eig(H)
+        order = torch.argsort(mu.abs())
+        mu, S = mu[order], S[:, order]
+        Y = V @ S.to(V.device)
+        R = op_shifted.apply(Y.T.contiguous()).reshape(kb, n).T - Y * mu.to(V.device)[None, :]
+        res = torch.linalg.vector_norm(R[:, :k], dim=0) / torch.clamp(mu[:k].abs().to(V.device), min=1e-300)
+        lam = (mu[:k] + shift).numpy()
+        vecs = Y[:, :k]
+        V, _ = torch.linalg.qr(Y)
+        if float(torch.max(torch.linalg.vector_norm(R[:, :k], dim=0))) <= tol * max(1.0, float(
+                torch.max(mu.abs()))) or float(res.max()) <= tol:
+            break
+    vecs = vecs / torch.linalg.vector_norm(vecs, dim=0, keepdim=True)
+    return lam, vecs

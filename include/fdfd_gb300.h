@@ -56,7 +56,15 @@ extern "C" {
  *              vectors: inv_sxf, inv_sxb (Nx each), inv_syf, inv_syb (Ny
  *              each), from fdfd_pml_sfactors (fdfdpy/pml.py:42-89).
  *   xlen/ylen: xrange[1]-xrange[0], yrange[1]-yrange[0] (grid spacing is
- *              xlen/Nx, ylen/Ny as in fdfdpy/linalg.py:25-33).           */
+ *              xlen/Nx, ylen/Ny as in fdfdpy/linalg.py:25-33).
+ *   stencil  : optional explicit 5-point operator, complex128 [5][Nx*Ny]
+ *              (centre, (i-1,j), (i+1,j), (i,j-1), (i,j+1) coefficients of
+ *              each row; neighbours wrap periodically).  When set, eps,
+ *              omega and the PML fields are not used for the coefficients
+ *              and any grid with Nx, Ny >= 1 is accepted (coupling to a
+ *              neighbour that coincides with the cell itself is added to
+ *              the diagonal).  The inv_s vectors may then be NULL; they are
+ *              only needed for transposed solves.                        */
 typedef struct fdfd_operator {
     int32_t Nx, Ny;
     int32_t pol;        /* FDFD_POL_EZ or FDFD_POL_HZ                    */
@@ -68,6 +76,7 @@ typedef struct fdfd_operator {
     const double *eps_add;
     const void   *diag_add;
     const void   *inv_sxf, *inv_sxb, *inv_syf, *inv_syb;
+    const void   *stencil;
 } fdfd_operator;
 
 /* ---- library ----------------------------------------------------------- */
@@ -114,6 +123,20 @@ int fdfd_apply(const fdfd_operator *op, const void *x, void *y,
  *   Ez: f1 = Hx, f2 = Hy;   Hz: f1 = Ex, f2 = Ey.                        */
 int fdfd_fields(const fdfd_operator *op, const void *X, void *f1, void *f2,
                 void *stream);
+
+/* ---- mode-source slice operator ---------------------------------------
+ * Writes the explicit stencil (see fdfd_operator.stencil, grid N x 1) of
+ * the 1-D periodic slice operator of insert_mode minus a shift:
+ *   Ez: omega^2 mu0' diag(eps0' eps) + Dxf Dxb - shift I     (mode.py:88)
+ *   Hz: omega^2 mu0' T_eps + T_eps Dxf T_epsx^-1 Dxb - shift I (mode.py:91)
+ * with raw periodic differences of spacing dl (mode.py:79-80) and
+ * T_epsx = eps0' * grid_average(eps slice, 'x') (mode.py:83), which
+ * averages along the slice only when `average` is nonzero (a slice normal
+ * to y; a slice normal to x is one row, so its 'x' average is eps itself).
+ * eps_slice: N float64 (device).  out: 5N complex128 (device).          */
+int fdfd_mode_stencil(int32_t N, int32_t pol, int32_t average,
+                      const double *eps_slice, double omega, double dl,
+                      double L0, double shift, void *out, void *stream);
 
 /* ---- K9: adjoint gradient ----------------------------------------------
  * dL/d(eps_r) = -omega^2 * eps0 * L0 * Re(lambda * E) (Ez), written to

@@ -298,3 +298,32 @@ def adjoint_grad_eps_Ez(A, E, g, omega, L0):
     (dA/deps_p = omega^2 eps0' e_p e_p^T from linalg.py:53-54, 66.)"""
     lam = spl.spsolve(A.T.tocsc(), np.conj(g).reshape(-1))
     return -(omega ** 2) * (EPSILON_0 * L0) * np.real(lam * E.reshape(-1))
+
+
+# ---- mode source (fdfdpy/source/mode.py:62-108) ------------------------------
+def mode_operator(pol, eps_slice, omega, dl, L0, average):
+    """The 1-D periodic slice operator of insert_mode (mode.py:76-91):
+    Ez: omega^2 mu0' T_eps + Dxf Dxb;  Hz: omega^2 mu0' T_eps + T_eps Dxf
+    T_epsx^-1 Dxb, raw periodic differences of spacing dl.  `average`
+    selects whether grid_average(eps, 'x') averages along the slice (a
+    slice normal to y) or returns eps (normal to x: one row)."""
+    e_sl = np.asarray(eps_slice, dtype=np.float64).reshape(-1)
+    Ns = e_sl.size
+    v = 1 / dl
+    I = np.arange(Ns)
+    Dxf = sp.csr_matrix((np.concatenate([-v * np.ones(Ns), v * np.ones(Ns)]),
+                         (np.concatenate([I, I]), np.concatenate([I, (I + 1) % Ns]))), shape=(Ns, Ns))
+    Dxb = sp.csr_matrix((np.concatenate([v * np.ones(Ns), -v * np.ones(Ns)]),
+                         (np.concatenate([I, I]), np.concatenate([I, (I - 1) % Ns]))), shape=(Ns, Ns))
+    EPS0_, MU0_ = EPSILON_0 * L0, MU_0 * L0
+    T_eps = sp.diags(EPS0_ * e_sl)
+    if pol == 'Ez':
+        return (np.square(omega) * MU0_ * T_eps + Dxf.dot(Dxb)).tocsr()
+    avg = (np.roll(e_sl, 1) + e_sl) / 2 if average else e_sl
+    T_inv = sp.diags((EPS0_ * avg) ** (-1))
+    return (np.square(omega) * MU0_ * T_eps + T_eps.dot(Dxf).dot(T_inv).dot(Dxb)).tocsr()
+
+
+def mode_eigs(A1, order, sigma):
+    """ARPACK shift-invert around sigma (linalg.py:110-119)."""
+    return spl.eigs(A1, k=order, sigma=sigma, which='LM')

@@ -162,7 +162,19 @@ def main():
     np.savez_compressed(OUT / "hz128_blocks.npz", eps=eps, Ex=Ex, Ey=Ey, Hz=Hz)
 
     # 5. mode source: the ridge waveguide of the examples notebook (Ez) and
-    #    an Hz variant; W_in, E2_in and the inserted source line
+    #    an Hz variant; W_in, E2_in and the inserted source line.  The
+    #    reference's slice operator and eigenpair are captured by wrapping
+    #    the solver_eigs it calls.
+    import fdfdpy.source.mode as M
+    captured = []
+    orig_eigs = M.solver_eigs
+
+    def recording_eigs(A, Neigs, guess_value=0, guess_vector=None, timing=False):
+        vals, vecs = orig_eigs(A, Neigs, guess_value=guess_value, guess_vector=guess_vector, timing=timing)
+        captured.append((A.toarray(), guess_value, vals.copy(), vecs.copy()))  # insert_mode scales vecs in place
+        return vals, vecs
+
+    M.solver_eigs = recording_eigs
     md = {}
     for pol in ("Ez", "Hz"):
         om = 2 * np.pi * 200e12
@@ -179,6 +191,21 @@ def main():
             # never fills, so only the source insertion is recorded for Hz.
             sim.modes[0].insert_mode(sim, sim.src)
         md[f"{pol.lower()}_src_line"] = sim.src[20, 70:130].copy()
+        A1, sig, vals, vecs = captured[-1]
+        md[f"{pol.lower()}_A1"] = A1
+        md[f"{pol.lower()}_sigma"] = sig
+        md[f"{pol.lower()}_eigval"] = vals
+        md[f"{pol.lower()}_eigvec"] = vecs
+    # a slice normal to y (its grid average runs along the slice)
+    eps = np.ones((200, 300))
+    eps[90:110, :] = 12.25
+    sim = Simulation(2 * np.pi * 200e12, eps, 0.01, [15, 15], "Hz")
+    sim.add_mode(3.5, "y", [100, 20], 60, scale=2)
+    sim.modes[0].insert_mode(sim, sim.src)
+    A1, sig, vals, vecs = captured[-1]
+    md["hzy_A1"], md["hzy_sigma"], md["hzy_eigval"], md["hzy_eigvec"] = A1, sig, vals, vecs
+    md["hzy_src_line"] = sim.src[70:130, 20].copy()
+    M.solver_eigs = orig_eigs
     np.savez_compressed(OUT / "modes.npz", **md)
 
     print("golden vectors written to", OUT)

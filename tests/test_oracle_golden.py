@@ -147,3 +147,24 @@ def test_superlu_complex64_refinement_converges():
         x = x + lu.solve((b - A @ x).astype(np.complex64)).astype(complex)
     assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) < 1e-10
     assert rel(x, g["Hz"].reshape(-1)) < 1e-8
+
+
+@pytest.mark.parametrize("tag,pol,average", [("ez", "Ez", False), ("hz", "Hz", False), ("hzy", "Hz", True)])
+def test_mode_operator_and_eigenpair(tag, pol, average):
+    m = np.load(GOLD / "modes.npz")
+    om = 2 * np.pi * 200e12
+    if tag == "hzy":
+        eps = np.ones((200, 300))
+        eps[90:110, :] = 12.25
+        sl = eps[70:130, 20]
+    else:
+        eps = np.ones((600, 200))
+        eps[:, 90:110] = 12.25
+        sl = eps[20, 70:130]
+    A1 = O.mode_operator(pol, sl, om, 0.01, 1e-6, average).toarray()
+    want = m[tag + "_A1"]
+    assert np.max(np.abs(A1 - want)) <= 1e-15 * np.max(np.abs(want))
+    vals, vecs = O.mode_eigs(O.mode_operator(pol, sl, om, 0.01, 1e-6, average), 1, float(m[tag + "_sigma"]))
+    assert abs(vals[0] - m[tag + "_eigval"][0]) <= 1e-10 * abs(vals[0])
+    v, w = vecs[:, 0], m[tag + "_eigvec"][:, 0]
+    assert min(np.linalg.norm(v - w), np.linalg.norm(v + w)) < 1e-8
