@@ -20,7 +20,7 @@ FDFD_ERR_NOT_CONVERGED = 5
 FDFD_ERR_NO_DEVICE = 6
 
 POL = {"Ez": 0, "Hz": 1}
-PREC = {"c128": 0, "c64": 1}
+PREC = {"c128": 0, "c64": 1, "c64tc": 2}
 
 
 class FDFDError(RuntimeError):
@@ -54,7 +54,7 @@ class SymbolicInfo(C.Structure):
 class FactorStats(C.Structure):
     _fields_ = [
         ("tiny_pivots", C.c_int32), ("refine_iters", C.c_int32), ("rel_residual", C.c_double),
-        ("factor_ms", C.c_double), ("solve_ms", C.c_double),
+        ("factor_ms", C.c_double), ("solve_ms", C.c_double), ("tc_errors", C.c_int32), ("pad", C.c_int32),
     ]
 
 

@@ -13,5 +13,5 @@ DEFAULT_LENGTH_SCALE = 1e-6  # microns
 # Engine defaults (no counterpart in the reference).
 DEFAULT_PRECISION = 'c128'   # the plain drop-in: complex128 factor
 DEFAULT_LEAF_AREA = 64       # nested-dissection leaf size (cells)
-DEFAULT_TOL = {'c128': 1e-12, 'c64': 1e-10}
-DEFAULT_MAX_REFINE = {'c128': 5, 'c64': 30}
+DEFAULT_TOL = {'c128': 1e-12, 'c64': 1e-10, 'c64tc': 1e-10}
+DEFAULT_MAX_REFINE = {'c128': 5, 'c64': 30, 'c64tc': 30}

@@ -30,10 +30,12 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "cplx.cuh"
 #include "profile.h"
+#include "schur_tc.h"
 #include "stencil.cuh"
 
 namespace fdfd {
@@ -554,6 +556,12 @@ struct fdfd_factor {
     int *d_tiny = nullptr;
     double *h_norm = nullptr;  // pinned
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // tensor-core Schur path (FDFD_PREC_C64_TC)
+    bool use_tc = false;
+    std::vector<char> tc_level;
+    TcFront *d_tcf = nullptr;
+    uint8_t *d_scratch = nullptr;
+    int *d_tcerr = nullptr;
     bool numeric_done = false;
     bool has_p = false;  // PML factors known: transposed solves allowed
     int Nx = 0, Ny = 0;
@@ -575,6 +583,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
     CUDA_TRY(cudaMemsetAsync(fac->d_pool, 0, (size_t)S.pool_entries * sizeof(T), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_tiny, 0, sizeof(int), st));
+    if (fac->d_tcerr) CUDA_TRY(cudaMemsetAsync(fac->d_tcerr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_maxdiag, 0, sizeof(unsigned long long), st));
     prof_begin(PROF_ASSEMBLE, st);
     k_maxdiag<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_maxdiag);
@@ -614,8 +623,15 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             k_gemm<T, R, TRSM_U><<<dim3(nfl, 1, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
             prof_end(PROF_TRSM, st, 2);
             prof_begin(PROF_SCHUR, st);
-            k_gemm<T, R, SCHUR><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
-            prof_end(PROF_SCHUR, st, 1);
+            if (std::is_same<T, c64>::value && fac->use_tc && fac->tc_level[L]) {
+                int rc = tc_schur_step(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch,
+                                       fac->d_tcerr, st);
+                if (rc) return rc;
+                prof_end(PROF_SCHUR, st, 3);
+            } else {
+                k_gemm<T, R, SCHUR><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+                prof_end(PROF_SCHUR, st, 1);
+            }
         }
     }
     CUDA_TRY(cudaGetLastError());
@@ -704,7 +720,7 @@ int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, in
     k_scales<<<1, 32, 0, st>>>(fac->d_norm, fac->d_maxdiag, nrhs, fac->d_sin, fac->d_sout);
     k_colscale<<<grid1(n * nrhs), 256, 0, st>>>(src, tmp, fac->d_sin, n, nrhs);
     prof_end(PROF_OTHER, st, 4 + (transpose ? 1 : 0));
-    if (fac->precision == FDFD_PREC_C64)
+    if (fac->precision != FDFD_PREC_C128)
         rc = solve_levels<c64, float>(fac, tmp, out, nrhs, st);
     else
         rc = solve_levels<c128, double>(fac, tmp, out, nrhs, st);
@@ -723,7 +739,8 @@ void free_factor(fdfd_factor *f) {
     if (!f) return;
     void *ptrs[] = {f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
-                    f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny};
+                    f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
+                    f->d_tcf, f->d_scratch, f->d_tcerr};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -732,8 +749,40 @@ void free_factor(fdfd_factor *f) {
     delete f;
 }
 
+// Tensor-core levels: fronts large enough for 128-row tiles to pay.
+constexpr int kTcMinM = 512;
+
+int64_t tc_layout(const Symbolic &S, std::vector<char> *lev, std::vector<TcFront> *tf) {
+    int64_t best = 0;
+    if (lev) lev->assign(S.nlev, 0);
+    if (tf) tf->assign(S.nf, TcFront{});
+    for (int L = 0; L < S.nlev; ++L) {
+        if (S.lev_max_m[L] < kTcMinM) continue;
+        if (lev) (*lev)[L] = 1;
+        int64_t off = 0;
+        for (int f = S.level_ptr[L]; f < S.level_ptr[L + 1]; ++f) {
+            int64_t ab = 0;
+            const int64_t tot = tc_front_scratch(S.m[f], S.p[f], &ab);
+            if (tf) {
+                (*tf)[f].a_off = off;
+                (*tf)[f].b_off = off + ab;
+            }
+            off += tot;
+        }
+        best = std::max(best, off);
+    }
+    if (tf)
+        for (int f = 0; f < S.nf; ++f) {
+            (*tf)[f].f_off = S.pool_off[f];
+            (*tf)[f].m = S.m[f];
+            (*tf)[f].p = S.p[f];
+            (*tf)[f].ld = S.ld[f];
+        }
+    return best;
+}
+
 int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
-    const int64_t elem = precision == FDFD_PREC_C64 ? 8 : 16;
+    const int64_t elem = precision == FDFD_PREC_C128 ? 16 : 8;
     const int64_t n = (int64_t)S.Nx * S.Ny;
     int64_t b = S.pool_entries * elem;
     b += 2 * S.sum_m * max_nrhs * elem;                  // W, Y
@@ -742,6 +791,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += 2 * S.sum_m * 4 + 6 * n * 4;                    // vars, relmap, nbr, var maps
     b += (int64_t)(S.Nx + S.Ny) * 16;
     b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
+    if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
     return b;
 }
 
@@ -751,7 +801,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
 extern "C" int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision, int32_t max_nrhs,
                                  int64_t *bytes) {
     if (!sym || !bytes) return fail(FDFD_ERR_BAD_ARG, "factor_bytes: NULL argument");
-    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64)
+    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64 && precision != FDFD_PREC_C64_TC)
         return fail(FDFD_ERR_BAD_ARG, "factor_bytes: unknown precision");
     if (max_nrhs < 1 || max_nrhs > 8) return fail(FDFD_ERR_BAD_ARG, "factor_bytes: max_nrhs must be 1..8");
     *bytes = factor_bytes_of(sym->s, precision, max_nrhs);
@@ -762,7 +812,7 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
                                   fdfd_factor **out) {
     if (!sym || !out) return fail(FDFD_ERR_BAD_ARG, "factor_create: NULL argument");
     *out = nullptr;
-    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64)
+    if (precision != FDFD_PREC_C128 && precision != FDFD_PREC_C64 && precision != FDFD_PREC_C64_TC)
         return fail(FDFD_ERR_BAD_ARG, "factor_create: unknown precision");
     if (max_nrhs < 1 || max_nrhs > 8) return fail(FDFD_ERR_BAD_ARG, "factor_create: max_nrhs must be 1..8");
     const Symbolic &S = sym->s;
@@ -776,7 +826,8 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
     f->sym = sym;
     f->precision = precision;
     f->max_nrhs = max_nrhs;
-    f->elem = precision == FDFD_PREC_C64 ? 8 : 16;
+    f->elem = precision == FDFD_PREC_C128 ? 16 : 8;
+    f->use_tc = precision == FDFD_PREC_C64_TC;
     f->n = (int64_t)S.Nx * S.Ny;
     f->Nx = S.Nx;
     f->Ny = S.Ny;
@@ -833,7 +884,20 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         free_factor(f);
         return fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
     }
-    int rc = (precision == FDFD_PREC_C64) ? set_smem_attrs<c64, float>() : set_smem_attrs<c128, double>();
+    int rc = (precision != FDFD_PREC_C128) ? set_smem_attrs<c64, float>() : set_smem_attrs<c128, double>();
+    if (rc == FDFD_OK && f->use_tc) {
+        std::vector<TcFront> tf;
+        const int64_t sb = tc_layout(S, &f->tc_level, &tf);
+        if (!alloc((void **)&f->d_tcf, S.nf * sizeof(TcFront)) || !alloc((void **)&f->d_scratch, sb) ||
+            !alloc((void **)&f->d_tcerr, 4)) {
+            free_factor(f);
+            return fail(FDFD_ERR_OOM, "factor_create: tensor-core scratch allocation failed");
+        }
+        e = cudaMemcpy(f->d_tcf, tf.data(), S.nf * sizeof(TcFront), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemset(f->d_tcerr, 0, 4);
+        if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+        if (rc == FDFD_OK) rc = tc_prepare();
+    }
     if (rc) {
         free_factor(f);
         return rc;
@@ -856,8 +920,8 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
         CUDA_TRY(cudaMemcpyAsync(fac->d_isyf, op->inv_syf, fac->Ny * 16, cudaMemcpyDeviceToDevice, st));
     }
     CUDA_TRY(cudaEventRecord(fac->ev[0], st));
-    rc = (fac->precision == FDFD_PREC_C64) ? factor_levels<c64, float>(fac, o, st)
-                                           : factor_levels<c128, double>(fac, o, st);
+    rc = (fac->precision != FDFD_PREC_C128) ? factor_levels<c64, float>(fac, o, st)
+                                            : factor_levels<c128, double>(fac, o, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[1], st));
     fac->numeric_done = true;
@@ -952,6 +1016,9 @@ extern "C" int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *
     int tiny = 0;
     if (f->numeric_done && cudaMemcpy(&tiny, f->d_tiny, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
         f->stats.tiny_pivots = tiny;
+    int tce = 0;
+    if (f->d_tcerr && cudaMemcpy(&tce, f->d_tcerr, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
+        f->stats.tc_errors = tce;
     *st = f->stats;
     return FDFD_OK;
 }

@@ -1,6 +1,8 @@
 // Kernel-class profiler of the engine (see profile.h).
 #include "profile.h"
 
+#include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -13,8 +15,9 @@ struct Pending {
     int cls;
     cudaEvent_t a, b;
 };
-bool g_enabled = false;
-long long g_launches[PROF_NCLASS] = {};
+std::atomic<bool> g_enabled{false};
+std::atomic<long long> g_launches[PROF_NCLASS];
+std::mutex g_mu;  // event bookkeeping (timing is meant for one stream at a time)
 double g_ms[PROF_NCLASS] = {};
 std::vector<Pending> g_pending;
 std::vector<cudaEvent_t> g_free;
@@ -34,6 +37,7 @@ cudaEvent_t take() {
 
 void prof_begin(int cls, cudaStream_t st) {
     if (!g_enabled) return;
+    std::lock_guard<std::mutex> lk(g_mu);
     cudaEvent_t e = take();
     cudaEventRecord(e, st);
     g_open[cls] = e;
@@ -41,7 +45,9 @@ void prof_begin(int cls, cudaStream_t st) {
 
 void prof_end(int cls, cudaStream_t st, int launches) {
     g_launches[cls] += launches;
-    if (!g_enabled || !g_open[cls]) return;
+    if (!g_enabled) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_open[cls]) return;
     cudaEvent_t e = take();
     cudaEventRecord(e, st);
     g_pending.push_back({cls, g_open[cls], e});
@@ -58,6 +64,7 @@ extern "C" int fdfd_profile_enable(int32_t on) {
 }
 
 extern "C" int fdfd_profile_reset(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
     for (int c = 0; c < PROF_NCLASS; ++c) {
         g_launches[c] = 0;
         g_ms[c] = 0.0;
@@ -72,6 +79,7 @@ extern "C" int fdfd_profile_reset(void) {
 
 extern "C" int fdfd_profile_read(int32_t nclass, double *ms, int64_t *launches) {
     if (nclass < 1 || !ms || !launches) return fail(FDFD_ERR_BAD_ARG, "profile_read: bad argument");
+    std::lock_guard<std::mutex> lk(g_mu);
     for (auto &p : g_pending) {
         if (cudaEventSynchronize(p.b) != cudaSuccess) {
             cudaGetLastError();

@@ -234,7 +234,7 @@ class Factor:
 
     def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1):
         if precision not in N.PREC:
-            raise ValueError("precision must be 'c128' or 'c64'")
+            raise ValueError("precision must be 'c128', 'c64' or 'c64tc'")
         device()
         self.sym, self.precision, self.max_nrhs = sym, precision, int(max_nrhs)
         h = C.c_void_p()
@@ -285,7 +285,8 @@ class Factor:
         st = N.FactorStats()
         N.call("fdfd_factor_stats_get", self.handle, C.byref(st))
         return {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
-                "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms}
+                "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
+                "tc_errors": st.tc_errors}
 
     def __del__(self):
         try:

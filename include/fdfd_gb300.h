@@ -44,6 +44,8 @@ extern "C" {
 
 #define FDFD_PREC_C128 0   /* plain: complex128 factor                    */
 #define FDFD_PREC_C64  1   /* mixed: complex64 factor + FP64 refinement   */
+#define FDFD_PREC_C64_TC 2 /* mixed, Schur updates of large fronts on the
+                              tcgen05 tensor cores (3xTF32 split)         */
 
 /* Operator description.  Mirrors the arguments of construct_A
  * (fdfdpy/linalg.py:41-44).  All pointers are DEVICE pointers.
@@ -196,6 +198,8 @@ typedef struct fdfd_factor_stats {
                             /* over right-hand sides)                     */
     double  factor_ms;      /* device time of the last factorization     */
     double  solve_ms;       /* device time of the last solve             */
+    int32_t tc_errors;      /* tensor-core tiles that timed out (0)       */
+    int32_t pad;
 } fdfd_factor_stats;
 
 int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision,

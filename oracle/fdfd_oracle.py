@@ -327,3 +327,52 @@ def mode_operator(pol, eps_slice, omega, dl, L0, average):
 def mode_eigs(A1, order, sigma):
     """ARPACK shift-invert around sigma (linalg.py:110-119)."""
     return spl.eigs(A1, k=order, sigma=sigma, which='LM')
+
+
+# ---- Kerr nonlinearity (fdfdpy/nonlinearity.py, nonlinear_solvers.py) ----------
+def kerr_terms(E, eps_r, chi, region, eps_scale=False, eps_max=None):
+    """eps_nl and dnl_de of one Kerr nonlinearity (nonlinearity.py:18-34);
+    chi already divided by L0^2 (simulation.py:72)."""
+    s = (eps_r - 1) / (eps_max - 1) if eps_scale else 1.0
+    return 3 * chi * region * np.square(np.abs(E)) * s, 3 * chi * region * np.conj(E) * s
+
+
+def solve_complex2real(A11, A12, b):
+    """[Re A11 + Re A12, -Im A11 + Im A12; Im A11 + Im A12, Re A11 - Re A12]
+    [xr; xi] = [br; bi] (linalg.py:152-186) by SuperLU."""
+    b = np.asarray(b).astype(np.complex128).reshape(-1)
+    n = b.size
+    R = sp.vstack((sp.hstack((A11.real + A12.real, -A11.imag + A12.imag)),
+                   sp.hstack((A11.imag + A12.imag, A11.real - A12.real)))).tocsc()
+    x = spl.spsolve(R, np.concatenate([b.real, b.imag]))
+    return x[:n] + 1j * x[n:]
+
+
+def newton_kerr_Ez(omega, xlen, ylen, eps_r, NPML, L0, src, chi, region, eps_scale=False, eps_max=None,
+                   conv_threshold=1e-10, max_num_iter=50):
+    """Newton iteration of newton_solve (nonlinear_solvers.py:57-115) for one
+    Kerr term, Ez, from the linear solution; returns (Ez_nl, conv list)
+    where Ez_nl is the final solve with the converged eps_nl."""
+    eps_r = np.asarray(eps_r, dtype=np.float64)
+    A = construct_A(omega, xlen, ylen, eps_r, NPML, 'Ez', L0)
+    b = (1j * omega * np.asarray(src)).reshape(-1).astype(np.complex128)
+    E = solve(A, b)
+    n = E.size
+    conv = []
+    e0 = EPSILON_0 * L0
+    for _ in range(max_num_iter):
+        eps_nl, dnl = kerr_terms(E, eps_r.reshape(-1), chi, region.reshape(-1), eps_scale, eps_max)
+        Anl = A + sp.diags(omega ** 2 * EPSILON_0 * L0 * eps_nl)
+        f = Anl @ E - b
+        dAde = dnl * omega ** 2 * e0
+        J11 = Anl + sp.diags(dAde * E)
+        J12 = sp.diags(np.conj(dAde) * E)
+        En = E - solve_complex2real(J11.tocsr(), J12.tocsr(), f)
+        c = np.linalg.norm(En - E) / np.linalg.norm(En)
+        conv.append(c)
+        E = En
+        if c < conv_threshold:
+            break
+    eps_nl, _ = kerr_terms(E, eps_r.reshape(-1), chi, region.reshape(-1), eps_scale, eps_max)
+    E_final = solve(A + sp.diags(omega ** 2 * EPSILON_0 * L0 * eps_nl), b)
+    return E_final, conv

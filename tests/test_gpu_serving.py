@@ -1,0 +1,61 @@
+"""The continuous-batching solve server: each result is the same alone and
+in the mix (bitwise: every request's arithmetic is independent of the
+others'), cached factors are reused, admission respects the memory
+budget, and every result meets its residual tolerance."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    from fdfdpy_gb300.serving import make_stream
+    reqs = make_stream(n_requests=10, rate=1e6, sides=(64, 96, 128, 160), reuse=0.3, seed=5, npml=(8, 8))
+    for r in reqs:
+        r.arrival = 0.0
+    return reqs
+
+
+def test_alone_equals_mix_and_meets_tolerance():
+    from fdfdpy_gb300.serving import SolveServer
+    alone = {}
+    for r in _requests():
+        srv = SolveServer(slots=1, precision="c64", tol=1e-10)
+        s = srv.run([r], realtime=False)
+        assert s["failed"] == 0
+        alone[r.rid] = r.x
+    mix = _requests()
+    srv = SolveServer(slots=4, precision="c64", tol=1e-10)
+    s = srv.run(mix, realtime=False)
+    assert s["failed"] == 0 and s["solves"] == sum(r.nrhs for r in mix)
+    assert s["max_rel_residual"] <= 1e-10
+    assert s["cache_hits"] >= 1
+    for r in mix:
+        a = alone[r.rid]
+        assert np.linalg.norm(r.x - a) <= 1e-12 * np.linalg.norm(a), r.rid
+
+
+def test_results_match_oracle():
+    from oracle import fdfd_oracle as O
+    from fdfdpy_gb300.serving import SolveServer
+    reqs = _requests()[:4]
+    SolveServer(slots=2, precision="c64", tol=1e-10).run(reqs, realtime=False)
+    for r in reqs:
+        N = r.eps_r.shape[0]
+        A = O.construct_A(r.omega, N * r.dl, N * r.dl, r.eps_r, list(r.NPML), r.pol, r.L0)
+        for k in range(r.nrhs):
+            assert np.linalg.norm(A @ r.x[k] - r.rhs[k]) <= 1e-10 * np.linalg.norm(r.rhs[k]) * 1.01
+
+
+def test_admission_budget_and_oversize_request():
+    from fdfdpy_gb300 import engine
+    from fdfdpy_gb300.serving import SolveServer
+    reqs = _requests()[:5]
+    need = max(engine.Factor.bytes_needed(engine.symbolic_for(*r.eps_r.shape), "c64", r.nrhs) for r in reqs)
+    srv = SolveServer(slots=4, precision="c64", memory_budget=int(need * 1.5), cache_budget=0)
+    s = srv.run(reqs, realtime=False)
+    assert s["failed"] == 0 and srv.resident == 0
+    big = _requests()[:1]
+    small_budget = SolveServer(slots=2, precision="c64", memory_budget=1024, cache_budget=0)
+    s = small_budget.run(big, realtime=False)
+    assert s["failed"] == 1 and "memory" in big[0].error
