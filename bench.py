@@ -211,6 +211,105 @@ def cpu_baseline_sample(n_side=512):
     return dt, dt * f_big / f_small, x
 
 
+def run_serving(args):
+    """Serving stream: Poisson arrivals, sides {128..1024}, Ez/Hz 50/50,
+    1-8 complex Gaussian RHS, eps 8x8 blocks, NPML 10, 25% eps reuse."""
+    import torch
+    from fdfdpy_gb300.serving import SolveServer, make_stream
+    reqs = make_stream(n_requests=args.requests, rate=args.rate, seed=0, npml=(10, 10), block=8)
+    warm = make_stream(n_requests=4, rate=1e6, seed=1, sides=(128, 256), npml=(10, 10), block=8)
+    SolveServer(slots=args.slots, precision=args.precision).run(warm, realtime=False)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        summ = SolveServer(slots=args.slots, precision=args.precision).run(reqs, realtime=True)
+    return {"metric": "serving solves/s with p50/p99 latency at rel. residual <=1e-10", "value": summ["solves_per_s"],
+            "unit": "solves/s", "higher_is_better": True, "dtype": "c64+f64" if args.precision != "c128" else "c128",
+            "data": "synthetic", "n_gpus": 1,
+            "config": {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, sides 128..1024, "
+                                   f"Ez/Hz 50/50, 1-8 RHS, eps 8x8 blocks, NPML 10, 25% eps reuse",
+                       "slots": args.slots, "precision": args.precision},
+            "serving": summ, "clocks": clk.summary()}
+
+
+def run_adjoint(args):
+    """Adjoint workload: Ez 600^2, NPML 20, centred 200^2 design region eps
+    U[1,12], src (100,300), J = |Ez(500,300)|^2; forward + backward timed."""
+    import torch
+    from fdfdpy_gb300.adjoint import solve_ez
+    rng = np.random.default_rng(0)
+    N = 600
+    eps = np.ones((N, N))
+    eps[200:400, 200:400] = rng.uniform(1, 12, size=(200, 200))
+    src = np.zeros((N, N))
+    src[100, 300] = 1
+    om = omega()
+    s = torch.tensor(src, device="cuda")
+    times = []
+    for i in range(args.warmup + args.steps):
+        e = torch.tensor(eps, device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        E = solve_ez(e, s, om, 0.02, [20, 20], precision=args.precision, tol=1e-10)
+        (E[500, 300].abs() ** 2).backward()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    v = 1.0 / float(np.mean(times))
+    return {"metric": "adjoint gradient evaluations/s (forward solve + backward transposed solve + K9)",
+            "value": v, "unit": "gradients/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "dtype": "c64+f64" if args.precision != "c128" else "c128",
+            "config": {"workload": "Ez 600x600 NPML 20, 200x200 design region eps U[1,12] seed 0, "
+                                   "J=|Ez(500,300)|^2", "precision": args.precision},
+            "ms_per_step": 1e3 / v}
+
+
+def run_kerr(args):
+    """Kerr Newton: Ez 1024^2, dl 0.02, NPML 20, centred 400^2 eps 12 with
+    chi3 2.8e-18 (zero elsewhere); point source amplitudes logspace(2,5,8)
+    solved as concurrent requests (one stream each); Newton to 1e-10."""
+    import torch
+    import threading
+    from fdfdpy_gb300 import Simulation
+    N = 1024
+    eps = np.ones((N, N))
+    eps[312:712, 312:712] = 12
+    region = np.zeros((N, N))
+    region[312:712, 312:712] = 1
+    om = omega()
+    amps = np.logspace(2, 5, 8)
+    results = {}
+
+    def one(k, a, stream):
+        with torch.cuda.stream(stream):
+            sim = Simulation(om, eps, 0.02, [20, 20], "Ez")
+            sim.precision = args.precision
+            sim.src[200, 512] = a
+            sim.add_nl(2.8e-18, region)
+            t0 = time.perf_counter()
+            out = sim.solve_fields_nl(solver_nl="newton", conv_threshold=1e-10, max_num_iter=args.newton_iters)
+            conv = out[3][:, 0]
+            nz = conv[conv > 0]
+            results[k] = {"amplitude": float(a), "newton_iters": int(nz.size),
+                          "final_change": float(nz[-1]) if nz.size else 0.0,
+                          "converged": bool(nz.size and nz[-1] < 1e-10), "s": time.perf_counter() - t0}
+
+    streams = [torch.cuda.Stream() for _ in amps]
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=one, args=(k, a, st)) for k, (a, st) in enumerate(zip(amps, streams))]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return {"metric": "Kerr Newton solves/s (8 amplitudes as concurrent requests)", "value": len(amps) / wall,
+            "unit": "nonlinear solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "dtype": "c64+f64" if args.precision != "c128" else "c128",
+            "config": {"workload": "Ez 1024x1024 dl 0.02 NPML 20, 400x400 eps 12 chi3 2.8e-18, src (200,512) "
+                                   "amplitudes logspace(2,5,8)", "precision": args.precision},
+            "wall_s": wall, "per_amplitude": [results[k] for k in sorted(results)]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -220,7 +319,17 @@ def main():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=512)
+    ap.add_argument("--workload", default="solve", choices=["solve", "serving", "adjoint", "kerr"])
+    ap.add_argument("--precision", default="c64")
+    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--rate", type=float, default=50.0)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--newton-iters", type=int, default=30)
     args = ap.parse_args()
+    if args.workload != "solve" and args.impl == "ours":
+        fn = {"serving": run_serving, "adjoint": run_adjoint, "kerr": run_kerr}[args.workload]
+        print(json.dumps(fn(args)))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
 
