@@ -434,6 +434,61 @@ __global__ void k_bwd_init(const FrontD *__restrict__ fr, const T *__restrict__ 
     (void)max_nrhs;
 }
 
+// Backward opener for fronts with a wide boundary, in two deterministic
+// passes.  Pass 1: CTA (front, row chunk, column chunk) writes the partial
+// product U[rows, cols] x_B[cols] of its 256 x 256 block to scratch; pass 2
+// sums the column chunks in a fixed order: acc = y - sum.  Scratch layout
+// per front: [col chunk][rhs][row] at bwd_off (elements).
+template <typename T>
+__global__ void k_bwd_partial(const FrontD *__restrict__ fr, const T *__restrict__ pool,
+                              const int32_t *__restrict__ vars, const double2 *__restrict__ x,
+                              const int64_t *__restrict__ bwd_off, T *scratch, int64_t n, int nrhs,
+                              int f_begin) {
+    extern __shared__ unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta
+    const int fi = f_begin + blockIdx.x;
+    const FrontD f = fr[fi];
+    const int rbase = blockIdx.y * kRowsPerCta, c0 = f.p + blockIdx.z * kRowsPerCta;
+    if (rbase >= f.p || c0 >= f.m) return;
+    const int cn = min(kRowsPerCta, f.m - c0);
+    const int32_t *v = vars + f.voff;
+    for (int idx = threadIdx.x; idx < cn * nrhs; idx += blockDim.x) {
+        const int r = idx / cn, cc = idx % cn;
+        const double2 xv = x[r * n + v[c0 + cc]];
+        xs[r * kRowsPerCta + cc] = from_c128<T>(xv, 1.0);
+    }
+    __syncthreads();
+    const int row = rbase + threadIdx.x;
+    if (row >= f.p) return;
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    T acc[8];
+    for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+    for (int cc = 0; cc < cn; ++cc) {
+        const T a = F[row + (int64_t)(c0 + cc) * ld];
+        for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, xs[r * kRowsPerCta + cc]);
+    }
+    T *out = scratch + bwd_off[fi] + ((int64_t)blockIdx.z * nrhs) * f.p;
+    for (int r = 0; r < nrhs; ++r) out[(int64_t)r * f.p + row] = acc[r];
+}
+
+template <typename T>
+__global__ void k_bwd_reduce(const FrontD *__restrict__ fr, const int64_t *__restrict__ bwd_off,
+                             const T *__restrict__ scratch, T *W, const T *__restrict__ Y, int64_t sum_m,
+                             int nrhs, int f_begin) {
+    const int fi = f_begin + blockIdx.x;
+    const FrontD f = fr[fi];
+    const int row = blockIdx.y * kRowsPerCta + threadIdx.x;
+    if (row >= f.p) return;
+    const int nch = (f.m - f.p + kRowsPerCta - 1) / kRowsPerCta;
+    const T *base = scratch + bwd_off[fi];
+    for (int r = 0; r < nrhs; ++r) {
+        T acc = Y[r * sum_m + f.voff + row];
+        for (int c = 0; c < nch; ++c) acc = csub(acc, base[((int64_t)c * nrhs + r) * f.p + row]);
+        W[r * sum_m + f.voff + row] = acc;
+    }
+}
+
 // Backward, one panel (descending k): x_k = inv(U_kk) acc_k, CTA 0 writes
 // x_k to the global solution, then acc[0:k0] -= U[0:k0, k] x_k.
 template <typename T, typename R>
@@ -556,6 +611,11 @@ struct fdfd_factor {
     int *d_tiny = nullptr;
     double *h_norm = nullptr;  // pinned
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // two-pass backward opener for levels with wide fronts
+    std::vector<char> bwd_wide;
+    int64_t *d_bwd_off = nullptr;
+    void *d_bwd_scratch = nullptr;
+    double pivot_tol = -1.0;  // relative static-pivot threshold (<0: default)
     // tensor-core Schur path (FDFD_PREC_C64_TC)
     bool use_tc = false;
     std::vector<char> tc_level;
@@ -590,7 +650,8 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc,
                                                        fac->d_nbr, fac->d_maxdiag, (T *)fac->d_pool);
     prof_end(PROF_ASSEMBLE, st, 2);
-    const R tiny = (R)std::sqrt((double)std::numeric_limits<R>::epsilon());
+    const R tiny = fac->pivot_tol >= 0.0 ? (R)fac->pivot_tol
+                                         : (R)std::sqrt((double)std::numeric_limits<R>::epsilon());
     T *pool = (T *)fac->d_pool;
     for (int L = 0; L < S.nlev; ++L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
@@ -666,9 +727,23 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         const int maxp = S.lev_max_p[L];
         const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
         prof_begin(PROF_SOLVE_BWD, st);
-        k_bwd_init<T><<<dim3(nfl, prow), kRowsPerCta, (size_t)nrhs * kRowsPerCta * sizeof(T), st>>>(
-            fac->d_fronts, pool, fac->d_vars, W, Y, x, fac->d_unit, sum_m, n, nrhs, fb, fac->max_nrhs);
-        int nl = 1;
+        int nbl = 1;
+        if (fac->bwd_wide[L]) {
+            int maxb = 0;
+            for (int f = fb; f < fb + nfl; ++f) maxb = std::max(maxb, S.m[f] - S.p[f]);
+            const int cch = (maxb + kRowsPerCta - 1) / kRowsPerCta;
+            k_bwd_partial<T><<<dim3(nfl, prow, cch), kRowsPerCta, (size_t)nrhs * kRowsPerCta * sizeof(T),
+                               st>>>(fac->d_fronts, pool, fac->d_vars, x, fac->d_bwd_off, (T *)fac->d_bwd_scratch,
+                                     n, nrhs, fb);
+            k_bwd_reduce<T><<<dim3(nfl, prow), kRowsPerCta, 0, st>>>(fac->d_fronts, fac->d_bwd_off,
+                                                                    (const T *)fac->d_bwd_scratch, W, Y, sum_m,
+                                                                    nrhs, fb);
+            nbl = 2;
+        } else {
+            k_bwd_init<T><<<dim3(nfl, prow), kRowsPerCta, (size_t)nrhs * kRowsPerCta * sizeof(T), st>>>(
+                fac->d_fronts, pool, fac->d_vars, W, Y, x, fac->d_unit, sum_m, n, nrhs, fb, fac->max_nrhs);
+        }
+        int nl = nbl;
         for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB, ++nl) {
             const int rows = std::max(1, (k0 + kRowsPerCta - 1) / kRowsPerCta);
             k_bwd_panel<T, R><<<dim3(nfl, rows), kRowsPerCta, sm_panel, st>>>(
@@ -740,7 +815,7 @@ void free_factor(fdfd_factor *f) {
     void *ptrs[] = {f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
-                    f->d_tcf, f->d_scratch, f->d_tcerr};
+                    f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -781,6 +856,29 @@ int64_t tc_layout(const Symbolic &S, std::vector<char> *lev, std::vector<TcFront
     return best;
 }
 
+// Levels whose fronts have a wide boundary use the two-pass backward
+// opener; returns the scratch elements it needs (per-level maximum).
+constexpr int kBwdWide = 512;
+int64_t bwd_layout(const Symbolic &S, int max_nrhs, std::vector<char> *wide, std::vector<int64_t> *off) {
+    int64_t best = 0;
+    if (wide) wide->assign(S.nlev, 0);
+    if (off) off->assign(S.nf, 0);
+    for (int L = 0; L < S.nlev; ++L) {
+        int maxb = 0;
+        for (int f = S.level_ptr[L]; f < S.level_ptr[L + 1]; ++f) maxb = std::max(maxb, S.m[f] - S.p[f]);
+        if (maxb < kBwdWide) continue;
+        if (wide) (*wide)[L] = 1;
+        int64_t o = 0;
+        for (int f = S.level_ptr[L]; f < S.level_ptr[L + 1]; ++f) {
+            if (off) (*off)[f] = o;
+            const int64_t nch = (S.m[f] - S.p[f] + kRowsPerCta - 1) / kRowsPerCta;
+            o += nch * max_nrhs * (int64_t)S.p[f];
+        }
+        best = std::max(best, o);
+    }
+    return best;
+}
+
 int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     const int64_t elem = precision == FDFD_PREC_C128 ? 16 : 8;
     const int64_t n = (int64_t)S.Nx * S.Ny;
@@ -792,6 +890,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += (int64_t)(S.Nx + S.Ny) * 16;
     b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
     if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
+    b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
     return b;
 }
 
@@ -898,11 +997,29 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
         if (rc == FDFD_OK) rc = tc_prepare();
     }
+    if (rc == FDFD_OK) {
+        std::vector<int64_t> boff;
+        const int64_t be = bwd_layout(S, max_nrhs, &f->bwd_wide, &boff);
+        if (!alloc((void **)&f->d_bwd_off, S.nf * sizeof(int64_t)) || !alloc(&f->d_bwd_scratch, be * f->elem)) {
+            free_factor(f);
+            return fail(FDFD_ERR_OOM, "factor_create: backward-solve scratch allocation failed");
+        }
+        e = cudaMemcpy(f->d_bwd_off, boff.data(), S.nf * sizeof(int64_t), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+    }
     if (rc) {
         free_factor(f);
         return rc;
     }
     *out = f;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol) {
+    if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_set_pivot_tol: NULL factor");
+    if (!(rel_tol >= 0.0) && rel_tol != -1.0)
+        return fail(FDFD_ERR_BAD_ARG, "factor_set_pivot_tol: tolerance must be >= 0 (or -1 for the default)");
+    fac->pivot_tol = rel_tol;
     return FDFD_OK;
 }
 

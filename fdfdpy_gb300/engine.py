@@ -232,7 +232,7 @@ def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
 class Factor:
     """A numeric multifrontal factorization of one operator on the device."""
 
-    def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1):
+    def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1, pivot_tol=None):
         if precision not in N.PREC:
             raise ValueError("precision must be 'c128', 'c64' or 'c64tc'")
         device()
@@ -240,6 +240,8 @@ class Factor:
         h = C.c_void_p()
         N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
         self.handle = h
+        if pivot_tol is not None:
+            N.call("fdfd_factor_set_pivot_tol", h, float(pivot_tol))
         self.op = None
 
     @staticmethod
