@@ -77,6 +77,7 @@ SIGNATURES = {
     "fdfd_adjoint_grad_eps": (C.c_int, [POP, P, P, P, P]),
     "fdfd_mode_stencil": (C.c_int, [I32, I32, I32, P, D, D, D, D, P, P]),
     "fdfd_norms": (C.c_int, [P, I64, I32, P, P]),
+    "fdfd_norms_noalloc": (C.c_int, [P, I64, I32, P, P]),
     "fdfd_symbolic_create": (C.c_int, [I32, I32, I32, C.POINTER(P)]),
     "fdfd_symbolic_info_get": (C.c_int, [P, C.POINTER(SymbolicInfo)]),
     "fdfd_symbolic_export": (C.c_int, [P, I32, P]),

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "stencil.cuh"
 
@@ -521,4 +522,63 @@ extern "C" int fdfd_mode_stencil(int32_t N, int32_t pol, int32_t average, const 
                                                                       EPSILON_0 * L0, v, shift,
                                                                       (double2 *)out);
     return launch_status("mode_stencil");
+}
+
+// ---- column norms without any device allocation -----------------------------
+// Some callers cannot allocate device memory at call time: a process whose
+// device memory is fully reserved by its own allocator (a serving loop with
+// a fixed budget, a framework's caching allocator holding the rest of HBM)
+// would see cudaMallocAsync fail or stall on allocator synchronisation in
+// the middle of an optimisation loop.  fdfd_norms_noalloc serves them from a
+// fixed scratch array in the library's static device memory instead; every
+// GPU that loads the library holds that array until the process exits.
+namespace {
+constexpr int kNoAllocMaxCols = 8;  // columns per call (documented limit)
+constexpr size_t kNoAllocDoubles = (size_t)kNormParts * kNoAllocMaxCols + kNoAllocMaxCols;
+static __device__ __align__(256) double g_norms_scratch[kNoAllocDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up
+// once per device (host code may not take the address of a __device__
+// symbol directly: the host-side name is only a stand-in).
+int noalloc_scratch(double **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(FDFD_ERR_NO_DEVICE, std::string("norms_noalloc: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(FDFD_ERR_BAD_ARG, "norms_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_norms_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(FDFD_ERR_CUDA, std::string("norms_noalloc: cudaGetSymbolAddress failed: ") +
+                                           cudaGetErrorString(e));
+        g_scratch_ptr[dev] = (double *)ptr;
+    }
+    *out = g_scratch_ptr[dev];
+    return FDFD_OK;
+}
+}  // namespace
+
+extern "C" int fdfd_norms_noalloc(const void *v, int64_t n, int32_t ncol, double *out_host, void *stream) {
+    if (!v || !out_host || n < 1 || ncol < 1) return fail(FDFD_ERR_BAD_ARG, "norms_noalloc: bad argument");
+    if (ncol > kNoAllocMaxCols)
+        return fail(FDFD_ERR_BAD_ARG, "norms_noalloc: at most " + std::to_string(kNoAllocMaxCols) +
+                                          " columns per call (fixed scratch); got " + std::to_string(ncol));
+    double *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    // Every partial-sum slot read by the final reduction is written by the
+    // first kernel of this same call, so nothing has to be cleared first.
+    double *partial = scratch, *out_dev = scratch + (size_t)kNormParts * kNoAllocMaxCols;
+    rc = norms_device(v, n, ncol, partial, out_dev, st);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(out_host, out_dev, ncol * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("norms_noalloc: ") + cudaGetErrorString(e));
+    return FDFD_OK;
 }

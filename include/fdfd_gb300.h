@@ -153,6 +153,23 @@ int fdfd_adjoint_grad_eps(const fdfd_operator *op, const void *lambda_,
 int fdfd_norms(const void *v, int64_t n, int32_t ncol, double *out_host,
                void *stream);
 
+/* Same column 2-norms as fdfd_norms, computed without allocating any device
+ * memory (fdfd_norms takes its partial-sum scratch from cudaMallocAsync).
+ * No counterpart in the reference: it exists for callers that cannot
+ * allocate at call time, such as a process whose device memory is held by
+ * its own allocator under a fixed budget.
+ *   - The scratch is one fixed array in the library's static device memory
+ *     (about 39 KB); every GPU that loads the library holds it until exit.
+ *   - At most 8 columns per call; more returns FDFD_ERR_BAD_ARG.
+ *   - The first call on a device looks up the array's device address (once
+ *     per device); make that first call before any stream capture.
+ *   - Every call shares the array: calls that overlap on the GPU (other
+ *     streams, other threads) race and must be serialised by the caller.
+ *   - Never calls cudaMalloc, cudaFree or an allocating library routine;
+ *     synchronises the stream to return the result in out_host.          */
+int fdfd_norms_noalloc(const void *v, int64_t n, int32_t ncol,
+                       double *out_host, void *stream);
+
 /* ---- symbolic analysis (host only) ------------------------------------
  * Geometric nested dissection of the periodic Nx x Ny grid (the graph of
  * construct_A's 5-point operator) into a front tree.  Replaces the fill-
