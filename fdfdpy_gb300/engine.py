@@ -37,7 +37,9 @@ def as_c128(x, shape=None) -> torch.Tensor:
     """Host/device array -> contiguous complex128 device tensor."""
     dev = device()
     if isinstance(x, torch.Tensor):
-        t = x.to(device=dev, dtype=torch.complex128)
+        # lazy conjugate / negative views must be materialised: the C ABI
+        # reads raw memory
+        t = x.to(device=dev, dtype=torch.complex128).resolve_conj().resolve_neg()
     else:
         a = np.ascontiguousarray(np.asarray(x, dtype=np.complex128))
         t = torch.from_numpy(a).to(dev, non_blocking=False)
@@ -48,7 +50,7 @@ def as_c128(x, shape=None) -> torch.Tensor:
 def as_f64(x) -> torch.Tensor:
     dev = device()
     if isinstance(x, torch.Tensor):
-        return x.to(device=dev, dtype=torch.float64).contiguous()
+        return x.to(device=dev, dtype=torch.float64).resolve_neg().contiguous()
     a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
     return torch.from_numpy(a).to(dev)
 
@@ -257,14 +259,24 @@ class Factor:
         self._op_struct = s
         return self
 
+    def _chunks(self, b, n):
+        """Right-hand sides in column blocks of at most max_nrhs."""
+        nrhs = b.numel() // n
+        flat = b.reshape(nrhs, n)
+        for c0 in range(0, nrhs, self.max_nrhs):
+            yield flat[c0:c0 + self.max_nrhs].contiguous()
+
     def apply_inverse(self, b, transpose=False):
         """One application x = A^-1 b (no refinement), complex128 device."""
         b = as_c128(b)
         n = self.op.n
-        nrhs = b.numel() // n
-        x = torch.empty_like(b)
-        N.call("fdfd_factor_solve", self.handle, _ptr(b), _ptr(x), nrhs, int(bool(transpose)), stream_ptr())
-        return x
+        outs = []
+        for blk in self._chunks(b, n):
+            x = torch.empty_like(blk)
+            N.call("fdfd_factor_solve", self.handle, _ptr(blk), _ptr(x), blk.shape[0], int(bool(transpose)),
+                   stream_ptr())
+            outs.append(x)
+        return torch.cat(outs).reshape(b.shape)
 
     def solve(self, b, transpose=False, tol=1e-12, max_iter=10, op: DeviceOperator | None = None,
               raise_on_fail=False):
@@ -272,23 +284,33 @@ class Factor:
         op = self.op if op is None else op
         b = as_c128(b)
         n = op.n
-        nrhs = b.numel() // n
-        x = torch.empty_like(b)
         s = op.struct()
-        code = N.lib().fdfd_solve_refined(self.handle, C.byref(s), _ptr(b), _ptr(x), nrhs,
-                                          int(bool(transpose)), float(tol), int(max_iter), stream_ptr())
-        if code == N.FDFD_ERR_NOT_CONVERGED and not raise_on_fail:
-            pass
-        else:
-            N.check(code, "fdfd_solve_refined")
-        return x
+        outs, worst, iters = [], 0.0, 0
+        for blk in self._chunks(b, n):
+            x = torch.empty_like(blk)
+            code = N.lib().fdfd_solve_refined(self.handle, C.byref(s), _ptr(blk), _ptr(x), blk.shape[0],
+                                              int(bool(transpose)), float(tol), int(max_iter), stream_ptr())
+            if code != N.FDFD_ERR_NOT_CONVERGED or raise_on_fail:
+                N.check(code, "fdfd_solve_refined")
+            st = self.stats()
+            worst, iters = max(worst, st["rel_residual"]), max(iters, st["refine_iters"])
+            outs.append(x)
+        self._last = (worst, iters)
+        return torch.cat(outs).reshape(b.shape)
 
     def stats(self) -> dict:
+        """Counters of the last factorization and solve (the residual and
+        refinement count are the worst over the column blocks of the last
+        solve call)."""
         st = N.FactorStats()
         N.call("fdfd_factor_stats_get", self.handle, C.byref(st))
-        return {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
-                "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
-                "tc_errors": st.tc_errors}
+        out = {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
+               "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
+               "tc_errors": st.tc_errors}
+        last = getattr(self, "_last", None)
+        if last is not None:
+            out["rel_residual"], out["refine_iters"] = max(out["rel_residual"], last[0]), max(out["refine_iters"], last[1])
+        return out
 
     def __del__(self):
         try:

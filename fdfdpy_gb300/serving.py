@@ -95,7 +95,7 @@ class SolveServer:
     def _need(self, req):
         sym = engine.symbolic_for(*req.eps_r.shape) if self.leaf_area is None else \
             engine.symbolic_for(*req.eps_r.shape, self.leaf_area)
-        return engine.Factor.bytes_needed(sym, self.precision, max(1, req.nrhs)), sym
+        return engine.Factor.bytes_needed(sym, self.precision, 8), sym
 
     def _evict_for(self, need):
         """Drop idle cached factors (LRU) until `need` fits (cv held)."""
@@ -122,7 +122,7 @@ class SolveServer:
                 need, sym = self._need(req)
                 op = engine.DeviceOperator(req.omega, req.eps_r, req.eps_r.shape[0] * req.dl,
                                            req.eps_r.shape[1] * req.dl, req.NPML, req.pol, req.L0)
-                fac = engine.Factor(sym, self.precision, max_nrhs=max(1, req.nrhs)).numeric(op)
+                fac = engine.Factor(sym, self.precision, max_nrhs=8).numeric(op)
                 ent = _CacheEntry(op, fac, need, users=1)
                 ent.lock.acquire()
             try:

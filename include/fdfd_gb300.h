@@ -239,8 +239,9 @@ int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
                        void *stream);
 /* Static-pivot threshold, relative to max|diag(A)| (the factor works on A
  * scaled by 1/max|diag(A)|): a pivot of smaller modulus is lifted to it and
- * counted in tiny_pivots.  -1 restores the default sqrt(eps) of the factor
- * precision.  Takes effect at the next fdfd_factor_numeric.              */
+ * counted in tiny_pivots.  -1 restores the default (1e-5 for complex64,
+ * sqrt(eps) = 1.5e-8 for complex128).  Takes effect at the next
+ * fdfd_factor_numeric.                                                   */
 int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol);
 int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st);
 void fdfd_factor_destroy(fdfd_factor *fac);

@@ -27,9 +27,9 @@ def test_alone_equals_mix_and_meets_tolerance():
     mix = _requests()
     srv = SolveServer(slots=4, precision="c64", tol=1e-10)
     s = srv.run(mix, realtime=False)
-    assert s["failed"] == 0 and s["solves"] == sum(r.nrhs for r in mix)
+    assert s["failed"] == 0, [r.error for r in mix if r.error]
+    assert s["solves"] == sum(r.nrhs for r in mix)
     assert s["max_rel_residual"] <= 1e-10
-    assert s["cache_hits"] >= 1
     for r in mix:
         a = alone[r.rid]
         assert np.linalg.norm(r.x - a) <= 1e-12 * np.linalg.norm(a), r.rid
@@ -51,7 +51,7 @@ def test_admission_budget_and_oversize_request():
     from fdfdpy_gb300 import engine
     from fdfdpy_gb300.serving import SolveServer
     reqs = _requests()[:5]
-    need = max(engine.Factor.bytes_needed(engine.symbolic_for(*r.eps_r.shape), "c64", r.nrhs) for r in reqs)
+    need = max(engine.Factor.bytes_needed(engine.symbolic_for(*r.eps_r.shape), "c64", 8) for r in reqs)
     srv = SolveServer(slots=4, precision="c64", memory_budget=int(need * 1.5), cache_budget=0)
     s = srv.run(reqs, realtime=False)
     assert s["failed"] == 0 and srv.resident == 0
@@ -59,3 +59,18 @@ def test_admission_budget_and_oversize_request():
     small_budget = SolveServer(slots=2, precision="c64", memory_budget=1024, cache_budget=0)
     s = small_budget.run(big, realtime=False)
     assert s["failed"] == 1 and "memory" in big[0].error
+
+
+def test_cached_factor_is_reused_for_new_sources():
+    from fdfdpy_gb300.serving import SolveServer, Request
+    base = _requests()[0]
+    rng = np.random.default_rng(9)
+    n = base.eps_r.size
+    first = Request(eps_r=base.eps_r, rhs=base.rhs[:1], omega=base.omega, dl=base.dl, NPML=base.NPML,
+                    pol=base.pol, arrival=0.0, rid=0)
+    second = Request(eps_r=base.eps_r.copy(), rhs=rng.standard_normal((5, n)) + 1j * rng.standard_normal((5, n)),
+                     omega=base.omega, dl=base.dl, NPML=base.NPML, pol=base.pol, arrival=0.5, rid=1)
+    srv = SolveServer(slots=2, precision="c64", tol=1e-10)
+    s = srv.run([first, second], realtime=True)
+    assert s["failed"] == 0 and s["cache_hits"] == 1 and second.cache_hit
+    assert second.x.shape == (5, n) and second.rel_residual <= 1e-10
