@@ -610,7 +610,15 @@ struct fdfd_factor {
     unsigned long long *d_maxdiag = nullptr;
     int *d_tiny = nullptr;
     double *h_norm = nullptr;  // pinned
+    int *h_err = nullptr;      // pinned copy of the solve error flag
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // cooperative per-level solves (levels with many panel steps)
+    std::vector<char> coop_level;
+    int coop_grid = 0;
+    void *d_bar = nullptr;
+    int *d_solve_err = nullptr;
+    int64_t *d_coop_off = nullptr;
+    void *d_coop_scratch = nullptr;
     // two-pass backward opener for levels with wide fronts
     std::vector<char> bwd_wide;
     int64_t *d_bwd_off = nullptr;
@@ -704,6 +712,212 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     return FDFD_OK;
 }
 
+// ---- cooperative per-level solves --------------------------------------------
+// Levels with many panel steps (the few large fronts near the root) run each
+// direction of the substitution as ONE cooperative launch: the grid walks
+// the panel steps itself, separated by a grid-wide barrier, instead of one
+// launch per step.  The barrier's wait is bounded: after kBarLimit polls a
+// CTA records an error and returns (the solve is then reported as failed).
+struct GridBar {
+    unsigned int count, gen;
+};
+constexpr unsigned kBarLimit = 1u << 24;
+
+__device__ bool grid_sync(GridBar *gb, int *err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int *vgen = &gb->gen;
+        const unsigned int g = *vgen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&gb->count, 1u) == gridDim.x - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            for (unsigned int it = 0; *vgen == g; ++it) {
+                if (it > kBarLimit) {
+                    ok = 0;
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(kRowsPerCta)
+    k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
+                const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+                const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
+                int *err) {
+    extern __shared__ unsigned char smem_raw[];
+    T *yk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
+    const int tid = threadIdx.x;
+    // gather: right-hand side of the pivots and the children's updates
+    for (int fi = blockIdx.x; fi < nfl; fi += gridDim.x) {
+        const FrontD f = fr[fb + fi];
+        const int32_t *v = vars + f.voff;
+        for (int r = 0; r < nrhs; ++r) {
+            T *w = W + r * sum_m + f.voff;
+            for (int k = tid; k < f.m; k += blockDim.x)
+                w[k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+        }
+        __syncthreads();
+        for (int slot = 0; slot < 2; ++slot) {
+            const int c = slot ? f.c1 : f.c0;
+            if (c < 0) continue;
+            const FrontD ch = fr[c];
+            const int mu = ch.m - ch.p;
+            const int32_t *rm = relmap + ch.voff + ch.p;
+            for (int r = 0; r < nrhs; ++r) {
+                T *w = W + r * sum_m + f.voff;
+                const T *wc = W + r * sum_m + ch.voff + ch.p;
+                for (int a = tid; a < mu; a += blockDim.x) w[rm[a]] = cadd(w[rm[a]], wc[a]);
+            }
+            __syncthreads();
+        }
+    }
+    if (!grid_sync(gb, err)) return;
+    for (int k0 = 0; k0 < maxp; k0 += NB) {
+        const int maxch = max(1, (maxm - k0 + kRowsPerCta - 1) / kRowsPerCta);
+        for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
+            const int fi = item / maxch, c = item % maxch;
+            const FrontD f = fr[fb + fi];
+            const int w = min(NB, f.p - k0);
+            if (w <= 0) continue;
+            const int t0 = k0 + w, rbase = t0 + c * kRowsPerCta;
+            if (c > 0 && rbase >= f.m) continue;
+            const T *F = pool + f.f_off;
+            const int64_t ld = f.ld;
+            for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+                const int r = idx / w, row = idx % w;
+                const T *wv = W + r * sum_m + f.voff + k0;
+                T acc = wv[row];
+                for (int t = 0; t < row; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], wv[t]);
+                yk[r * NB + row] = acc;
+            }
+            __syncthreads();
+            if (c == 0)
+                for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+                    const int r = idx / w, row = idx % w;
+                    Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
+                }
+            const int row = rbase + tid;
+            if (row < f.m)
+                for (int r = 0; r < nrhs; ++r) {
+                    T acc = czero<T>();
+                    for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], yk[r * NB + t]);
+                    T &dst = W[r * sum_m + f.voff + row];
+                    dst = csub(dst, acc);
+                }
+            __syncthreads();
+        }
+        if (!grid_sync(gb, err)) return;
+    }
+}
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(kRowsPerCta)
+    k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
+                const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
+                T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err) {
+    extern __shared__ unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta (also x_k: nrhs x NB)
+    const int tid = threadIdx.x;
+    const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
+    const int cch = max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
+    // opener, pass 1: partial products U[rows, cols] x_B[cols] per 256 x 256 block
+    for (int item = blockIdx.x; item < nfl * prow * cch; item += gridDim.x) {
+        const int fi = item / (prow * cch), rc = (item / cch) % prow, cc = item % cch;
+        const FrontD f = fr[fb + fi];
+        const int rbase = rc * kRowsPerCta, c0 = f.p + cc * kRowsPerCta;
+        if (rbase >= f.p || c0 >= f.m) continue;
+        const int cn = min(kRowsPerCta, f.m - c0);
+        const int32_t *v = vars + f.voff;
+        for (int idx = tid; idx < cn * nrhs; idx += blockDim.x) {
+            const int r = idx / cn, q = idx % cn;
+            xs[r * kRowsPerCta + q] = from_c128<T>(x[r * n + v[c0 + q]], 1.0);
+        }
+        __syncthreads();
+        const int row = rbase + tid;
+        if (row < f.p) {
+            const T *F = pool + f.f_off;
+            T acc[8];
+            for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+            for (int q = 0; q < cn; ++q) {
+                const T a = F[row + (int64_t)(c0 + q) * f.ld];
+                for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, xs[r * kRowsPerCta + q]);
+            }
+            T *out = scratch + bwd_off[fb + fi] + ((int64_t)cc * nrhs) * f.p;
+            for (int r = 0; r < nrhs; ++r) out[(int64_t)r * f.p + row] = acc[r];
+        }
+        __syncthreads();
+    }
+    if (!grid_sync(gb, err)) return;
+    // opener, pass 2: acc = y - sum of the column blocks, in a fixed order
+    for (int item = blockIdx.x; item < nfl * prow; item += gridDim.x) {
+        const int fi = item / prow, rc = item % prow;
+        const FrontD f = fr[fb + fi];
+        const int row = rc * kRowsPerCta + tid;
+        if (row < f.p) {
+            const int nch = (f.m - f.p + kRowsPerCta - 1) / kRowsPerCta;
+            const T *base = scratch + bwd_off[fb + fi];
+            for (int r = 0; r < nrhs; ++r) {
+                T acc = Y[r * sum_m + f.voff + row];
+                for (int c = 0; c < nch; ++c) acc = csub(acc, base[((int64_t)c * nrhs + r) * f.p + row]);
+                W[r * sum_m + f.voff + row] = acc;
+            }
+        }
+    }
+    if (!grid_sync(gb, err)) return;
+    for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
+        const int maxch = max(1, (k0 + kRowsPerCta - 1) / kRowsPerCta);
+        for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
+            const int fi = item / maxch, c = item % maxch;
+            const FrontD f = fr[fb + fi];
+            const int w = min(NB, f.p - k0);
+            if (w <= 0) continue;
+            const int rbase = c * kRowsPerCta;
+            if (c > 0 && rbase >= k0) continue;
+            const T *F = pool + f.f_off;
+            const int64_t ld = f.ld;
+            for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+                const int r = idx / w, row = idx % w;
+                const T *av = W + r * sum_m + f.voff + k0;
+                T acc = czero<T>();
+                for (int t = row; t < w; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], av[t]);
+                xs[r * NB + row] = acc;
+            }
+            __syncthreads();
+            if (c == 0) {
+                const int32_t *v = vars + f.voff + k0;
+                for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+                    const int r = idx / w, row = idx % w;
+                    x[r * n + v[row]] = to_c128(xs[r * NB + row], 1.0);
+                }
+            }
+            const int row = rbase + tid;
+            if (row < k0)
+                for (int r = 0; r < nrhs; ++r) {
+                    T acc = czero<T>();
+                    for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], xs[r * NB + t]);
+                    T &dst = W[r * sum_m + f.voff + row];
+                    dst = csub(dst, acc);
+                }
+            __syncthreads();
+        }
+        if (!grid_sync(gb, err)) return;
+    }
+}
+
 // x = A^-1 b for nrhs columns (b, x complex128 on device; may alias d_tmp).
 // s_in / s_out are device arrays of per-column scales.
 template <typename T, typename R>
@@ -713,9 +927,23 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
     const T *pool = (const T *)fac->d_pool;
     const int64_t sum_m = S.sum_m, n = fac->n;
     const size_t sm_panel = (size_t)nrhs * NB * sizeof(T);
+    CUDA_TRY(cudaMemsetAsync(fac->d_bar, 0, sizeof(GridBar), st));
+    const size_t sm_coop = (size_t)nrhs * kRowsPerCta * sizeof(T);
     for (int L = 0; L < S.nlev; ++L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
         prof_begin(PROF_SOLVE_FWD, st);
+        if (fac->coop_level[L]) {
+            int maxp = S.lev_max_p[L], maxm = S.lev_max_m[L];
+            GridBar *gb = (GridBar *)fac->d_bar;
+            int *err = fac->d_solve_err;
+            void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
+                            (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
+                            (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err};
+            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(fac->coop_grid),
+                                                 dim3(kRowsPerCta), args, sm_coop, st));
+            prof_end(PROF_SOLVE_FWD, st, 1);
+            continue;
+        }
         k_fwd_gather<T><<<nfl, 256, 0, st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, b, fac->d_unit,
                                              W, sum_m, n, nrhs, fb);
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
@@ -732,6 +960,21 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         const int maxp = S.lev_max_p[L];
         const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
         prof_begin(PROF_SOLVE_BWD, st);
+        if (fac->coop_level[L]) {
+            int maxpp = maxp, maxb = 0;
+            for (int f = fb; f < fb + nfl; ++f) maxb = std::max(maxb, S.m[f] - S.p[f]);
+            GridBar *gb = (GridBar *)fac->d_bar;
+            int *err = fac->d_solve_err;
+            T *scr = (T *)fac->d_coop_scratch;
+            void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxpp, (void *)&maxb,
+                            (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
+                            (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
+                            (void *)&gb, (void *)&err};
+            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(fac->coop_grid),
+                                                 dim3(kRowsPerCta), args, sm_coop, st));
+            prof_end(PROF_SOLVE_BWD, st, 1);
+            continue;
+        }
         int nbl = 1;
         if (fac->bwd_wide[L]) {
             int maxb = 0;
@@ -820,10 +1063,12 @@ void free_factor(fdfd_factor *f) {
     void *ptrs[] = {f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
-                    f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch};
+                    f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
+                    f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
+    if (f->h_err) cudaFreeHost(f->h_err);
     for (auto &e : f->ev)
         if (e) cudaEventDestroy(e);
     delete f;
@@ -884,6 +1129,28 @@ int64_t bwd_layout(const Symbolic &S, int max_nrhs, std::vector<char> *wide, std
     return best;
 }
 
+// Levels with at least kCoopPanels panel steps run their substitutions as
+// cooperative launches; their opener scratch (per front: column blocks x
+// rhs x p) is laid out here.
+constexpr int kCoopPanels = 4;
+int64_t coop_layout(const Symbolic &S, int max_nrhs, std::vector<char> *lev, std::vector<int64_t> *off) {
+    int64_t best = 0;
+    if (lev) lev->assign(S.nlev, 0);
+    if (off) off->assign(S.nf, 0);
+    for (int L = 0; L < S.nlev; ++L) {
+        if ((S.lev_max_p[L] + NB - 1) / NB < kCoopPanels) continue;
+        if (lev) (*lev)[L] = 1;
+        int64_t o = 0;
+        for (int f = S.level_ptr[L]; f < S.level_ptr[L + 1]; ++f) {
+            if (off) (*off)[f] = o;
+            const int64_t nch = std::max<int64_t>(1, (S.m[f] - S.p[f] + kRowsPerCta - 1) / kRowsPerCta);
+            o += nch * max_nrhs * (int64_t)S.p[f];
+        }
+        best = std::max(best, o);
+    }
+    return best;
+}
+
 int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     const int64_t elem = precision == FDFD_PREC_C128 ? 16 : 8;
     const int64_t n = (int64_t)S.Nx * S.Ny;
@@ -896,11 +1163,30 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
     if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
     b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
+    b += coop_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8 + 16;
     return b;
 }
 
 }  // namespace
 }  // namespace fdfd
+
+template <typename T, typename R>
+int coop_grid_for(int max_nrhs, int *grid) {
+    int dev = 0, sms = 0, coop = 0, nb1 = 0, nb2 = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) {
+        *grid = 0;
+        return FDFD_OK;
+    }
+    const size_t smem = (size_t)max_nrhs * kRowsPerCta * sizeof(T);
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_fwd_level<T, R>, kRowsPerCta, smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_bwd_level<T, R>, kRowsPerCta, smem));
+    const int per_sm = std::min(std::min(nb1, nb2), 2);
+    *grid = per_sm > 0 ? per_sm * sms : 0;
+    return FDFD_OK;
+}
 
 extern "C" int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision, int32_t max_nrhs,
                                  int64_t *bytes) {
@@ -974,6 +1260,7 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         return fail(FDFD_ERR_OOM, "factor_create: device allocation failed");
     }
     cudaError_t e = cudaMallocHost((void **)&f->h_norm, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&f->h_err, sizeof(int));
     for (auto &ev : f->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
     const double ones[8] = {1, 1, 1, 1, 1, 1, 1, 1};
@@ -1001,6 +1288,24 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         if (e == cudaSuccess) e = cudaMemset(f->d_tcerr, 0, 4);
         if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
         if (rc == FDFD_OK) rc = tc_prepare();
+    }
+    if (rc == FDFD_OK) {
+        std::vector<int64_t> coff;
+        const int64_t ce = coop_layout(S, max_nrhs, &f->coop_level, &coff);
+        rc = (precision != FDFD_PREC_C128) ? coop_grid_for<c64, float>(max_nrhs, &f->coop_grid)
+                                           : coop_grid_for<c128, double>(max_nrhs, &f->coop_grid);
+        if (rc == FDFD_OK && f->coop_grid == 0) f->coop_level.assign(S.nlev, 0);  // no cooperative launch
+        if (rc == FDFD_OK &&
+            (!alloc(&f->d_bar, sizeof(GridBar)) || !alloc((void **)&f->d_solve_err, 4) ||
+             !alloc((void **)&f->d_coop_off, S.nf * sizeof(int64_t)) || !alloc(&f->d_coop_scratch, ce * f->elem))) {
+            free_factor(f);
+            return fail(FDFD_ERR_OOM, "factor_create: cooperative-solve scratch allocation failed");
+        }
+        if (rc == FDFD_OK) {
+            e = cudaMemcpy(f->d_coop_off, coff.data(), S.nf * sizeof(int64_t), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemset(f->d_solve_err, 0, 4);
+            if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+        }
     }
     if (rc == FDFD_OK) {
         std::vector<int64_t> boff;
@@ -1057,6 +1362,7 @@ extern "C" int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x, int32
     if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "factor_solve: nrhs out of range");
     cudaStream_t st = (cudaStream_t)stream;
     CUDA_TRY(cudaEventRecord(fac->ev[2], st));
+    CUDA_TRY(cudaMemsetAsync(fac->d_solve_err, 0, sizeof(int), st));
     int rc = apply_factor(fac, (const double2 *)b, (double2 *)x, nrhs, transpose, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[3], st));
@@ -1080,6 +1386,7 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
     const double2 *bb = (const double2 *)b;
     double2 *xx = (double2 *)x;
     CUDA_TRY(cudaEventRecord(fac->ev[2], st));
+    CUDA_TRY(cudaMemsetAsync(fac->d_solve_err, 0, sizeof(int), st));
     double bnorm[8];
     prof_begin(PROF_OTHER, st);
     rc = norms_device(bb, n, nrhs, fac->d_partial, fac->d_norm, st);
@@ -1101,7 +1408,10 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
         if (rc) return rc;
         prof_end(PROF_OTHER, st, 3);
         CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
+        if (*fac->h_err)
+            return fail(FDFD_ERR_CUDA, "solve_refined: a grid barrier of the cooperative solve timed out");
         worst = 0.0;
         for (int r = 0; r < nrhs; ++r) {
             const double rel = bnorm[r] > 0 ? fac->h_norm[r] / bnorm[r] : fac->h_norm[r];
