@@ -190,23 +190,48 @@ __global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, i
         }
         __syncthreads();
     }
-    // inv(L) column by column (threads 0..w-1), inv(U) row by row
-    // (threads w..2w-1).  Both land in X without overlap.
-    if (tid < w) {
-        const int c = tid;
-        for (int r = c + 1; r < w; ++r) {
-            T acc = D[r + c * NB];
-            for (int t = c + 1; t < r; ++t) cmac(acc, D[r + t * NB], X[t + c * NB]);
-            X[r + c * NB] = cmake<R>(-acc.x, -acc.y);
-        }
-    } else if (tid < 2 * w) {
-        const int r = tid - w;
-        X[r + r * NB] = crecip(D[r + r * NB]);
-        for (int c = r + 1; c < w; ++c) {
-            T acc = czero<T>();
-            for (int t = r; t < c; ++t) cmac(acc, X[r + t * NB], D[t + c * NB]);
-            const T q = cmul(acc, crecip(D[c + c * NB]));
-            X[r + c * NB] = cmake<R>(-q.x, -q.y);
+    // inv(L) (unit lower) and inv(U), warp-parallel: a warp owns whole
+    // columns of inv(L) / rows of inv(U), two entries per lane in registers,
+    // and advances one step per shuffle (axpy form of the substitution).
+    const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
+    for (int job = warp; job < 2 * w; job += nwarps) {
+        if (job < w) {
+            // column c of inv(L): x = e_c; for t >= c: x[t+1:] -= L[t+1:, t] x[t]
+            const int c = job;
+            T x0 = (lane == c) ? cone<T>() : czero<T>();
+            T x1 = (lane + 32 == c) ? cone<T>() : czero<T>();
+            for (int t = c; t < w - 1; ++t) {
+                const T own = (t < 32) ? x0 : x1;
+                T xt;
+                xt.x = __shfl_sync(0xffffffffu, own.x, t & 31);
+                xt.y = __shfl_sync(0xffffffffu, own.y, t & 31);
+                if (lane > t && lane < w) cmsub(x0, D[lane + t * NB], xt);
+                if (lane + 32 > t && lane + 32 < w) cmsub(x1, D[lane + 32 + t * NB], xt);
+            }
+            if (lane > c && lane < w) X[lane + c * NB] = x0;
+            if (lane + 32 > c && lane + 32 < w) X[lane + 32 + c * NB] = x1;
+        } else {
+            // row r of inv(U): y U = e_r; for c >= r: y[c] = (e_r[c] - a[c]) / U[c,c],
+            // then a[c+1:] += y[c] U[c, c+1:]
+            const int r = job - w;
+            T a0 = czero<T>(), a1 = czero<T>();
+            T y0 = czero<T>(), y1 = czero<T>();
+            for (int c = r; c < w; ++c) {
+                const bool mine0 = (lane == c), mine1 = (lane + 32 == c);
+                T yc = czero<T>();
+                if (mine0 || mine1) {
+                    const T ac = mine0 ? a0 : a1;
+                    const T num = cmake<R>((c == r ? R(1) : R(0)) - ac.x, -ac.y);
+                    yc = cmul(num, crecip(D[c + c * NB]));
+                    if (mine0) y0 = yc; else y1 = yc;
+                }
+                yc.x = __shfl_sync(0xffffffffu, yc.x, c & 31);
+                yc.y = __shfl_sync(0xffffffffu, yc.y, c & 31);
+                if (lane > c && lane < w) cmac(a0, yc, D[c + lane * NB]);
+                if (lane + 32 > c && lane + 32 < w) cmac(a1, yc, D[c + (lane + 32) * NB]);
+            }
+            if (lane >= r && lane < w) X[r + lane * NB] = y0;
+            if (lane + 32 >= r && lane + 32 < w) X[r + (lane + 32) * NB] = y1;
         }
     }
     __syncthreads();
@@ -357,13 +382,87 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
     }
 }
 
+// ---- shared panel-step helpers of the triangular solves ------------------------
+// Shared memory of one panel step: the w x w diagonal block (only its
+// triangle), the input vector block and the result block, staged with
+// coalesced loads so that the dependent triangular product runs out of
+// shared memory instead of waiting on a global load per term.
+constexpr int kPanelSmemElems = NB * NB;  // + 2 * nrhs * NB
+template <typename T>
+__host__ __device__ __forceinline__ size_t panel_smem_bytes(int nrhs) {
+    return (size_t)(NB * NB + 2 * nrhs * NB) * sizeof(T);
+}
+
+// out = inv(L_kk) v (UPPER = false: unit lower inverse stored strictly below
+// the diagonal) or out = inv(U_kk) v (UPPER = true: on and above).  v is
+// read from vin_g (per rhs stride vstride); result left in sm (returned).
+template <typename T, typename R, bool UPPER>
+__device__ __forceinline__ T *panel_diag_apply(const T *F, int64_t ld, int k0, int w, const T *vin_g,
+                                               int64_t vstride, int nrhs, T *sm) {
+    T *Ds = sm, *vin = sm + NB * NB, *out = vin + nrhs * NB;
+    const int tid = threadIdx.x;
+    for (int idx = tid; idx < w * w; idx += blockDim.x) {
+        const int r = idx % w, c = idx / w;
+        const bool need = UPPER ? (r <= c) : (r > c);
+        Ds[r + c * NB] = need ? F[(k0 + r) + (int64_t)(k0 + c) * ld] : czero<T>();
+    }
+    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+        const int r = idx / w, i = idx % w;
+        vin[r * NB + i] = vin_g[r * vstride + k0 + i];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
+        const int r = idx / w, row = idx % w;
+        const T *vr = vin + r * NB;
+        T acc;
+        if (UPPER) {
+            acc = czero<T>();
+            for (int t = row; t < w; ++t) cmac(acc, Ds[row + t * NB], vr[t]);
+        } else {
+            acc = vr[row];
+            for (int t = 0; t < row; ++t) cmac(acc, Ds[row + t * NB], vr[t]);
+        }
+        out[r * NB + row] = acc;
+    }
+    __syncthreads();
+    return out;
+}
+
+// dst[row] -= F[row, k0:k0+w] y for one row and all right-hand sides.
+template <typename T>
+__device__ __forceinline__ void panel_row_update(const T *F, int64_t ld, int k0, int w, int row, const T *y,
+                                                 int nrhs, T *dst, int64_t dstride) {
+    T acc[8];
+    for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+    const T *Fr = F + row + (int64_t)k0 * ld;
+    int t = 0;
+    for (; t + 4 <= w; t += 4) {
+        const T a0 = Fr[(int64_t)t * ld], a1 = Fr[(int64_t)(t + 1) * ld];
+        const T a2 = Fr[(int64_t)(t + 2) * ld], a3 = Fr[(int64_t)(t + 3) * ld];
+        for (int r = 0; r < nrhs; ++r) {
+            const T *yr = y + r * NB + t;
+            cmac(acc[r], a0, yr[0]);
+            cmac(acc[r], a1, yr[1]);
+            cmac(acc[r], a2, yr[2]);
+            cmac(acc[r], a3, yr[3]);
+        }
+    }
+    for (; t < w; ++t) {
+        const T a = Fr[(int64_t)t * ld];
+        for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, y[r * NB + t]);
+    }
+    for (int r = 0; r < nrhs; ++r) {
+        T &d = dst[r * dstride + row];
+        d = csub(d, acc[r]);
+    }
+}
+
 // Forward, one panel: y_k = inv(L_kk) w_k (every CTA of the front computes
 // it; CTA 0 stores it to Y), then w[t0:m] -= L[t0:m, k] y_k.
 template <typename T, typename R>
 __global__ void k_fwd_panel(const FrontD *__restrict__ fr, const T *__restrict__ pool, T *W, T *Y,
                             int64_t sum_m, int nrhs, int f_begin, int k0) {
     extern __shared__ unsigned char smem_raw[];
-    T *yk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
@@ -371,30 +470,16 @@ __global__ void k_fwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
     const int rbase = t0 + blockIdx.y * kRowsPerCta;
     if (blockIdx.y > 0 && rbase >= f.m) return;
     const T *F = pool + f.f_off;
-    const int64_t ld = f.ld;
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-        const int r = idx / w, row = idx % w;
-        const T *wv = W + r * sum_m + f.voff + k0;
-        T acc = wv[row];
-        for (int t = 0; t < row; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], wv[t]);
-        yk[r * NB + row] = acc;
-    }
-    __syncthreads();
+    T *yk = panel_diag_apply<T, R, false>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
+                                          reinterpret_cast<T *>(smem_raw));
     if (blockIdx.y == 0)
         for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
             const int r = idx / w, row = idx % w;
             Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
         }
     const int row = rbase + tid;
-    if (row < f.m) {
-        for (int r = 0; r < nrhs; ++r) {
-            T acc = czero<T>();
-            for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], yk[r * NB + t]);
-            T &dst = W[r * sum_m + f.voff + row];
-            dst = csub(dst, acc);
-        }
-    }
+    if (row < f.m) panel_row_update(F, f.ld, k0, w, row, yk, nrhs, W + f.voff, sum_m);
 }
 
 // Backward, step 1: acc[0:p] = y[0:p] - U[0:p, p:m] x_B, x_B read from the
@@ -497,23 +582,15 @@ __global__ void k_bwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
                             const double *__restrict__ s_out, int64_t sum_m, int64_t n, int nrhs,
                             int f_begin, int k0) {
     extern __shared__ unsigned char smem_raw[];
-    T *xk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
     const int rbase = blockIdx.y * kRowsPerCta;
     if (blockIdx.y > 0 && rbase >= k0) return;
     const T *F = pool + f.f_off;
-    const int64_t ld = f.ld;
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-        const int r = idx / w, row = idx % w;
-        const T *av = W + r * sum_m + f.voff + k0;
-        T acc = czero<T>();
-        for (int t = row; t < w; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], av[t]);
-        xk[r * NB + row] = acc;
-    }
-    __syncthreads();
+    T *xk = panel_diag_apply<T, R, true>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
+                                         reinterpret_cast<T *>(smem_raw));
     if (blockIdx.y == 0) {
         const int32_t *v = vars + f.voff + k0;
         for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
@@ -522,14 +599,7 @@ __global__ void k_bwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
         }
     }
     const int row = rbase + tid;
-    if (row < k0) {
-        for (int r = 0; r < nrhs; ++r) {
-            T acc = czero<T>();
-            for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], xk[r * NB + t]);
-            T &dst = W[r * sum_m + f.voff + row];
-            dst = csub(dst, acc);
-        }
-    }
+    if (row < k0) panel_row_update(F, f.ld, k0, w, row, xk, nrhs, W + f.voff, sum_m);
 }
 
 // Per-column solve scales: s_in = 1/||r||, s_out = sigma ||r||.
@@ -639,12 +709,6 @@ struct fdfd_factor {
 namespace fdfd {
 namespace {
 
-template <typename T, typename R>
-int set_smem_attrs() {
-    CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(2 * NB * NB * sizeof(T))));
-    return FDFD_OK;
-}
 
 template <typename T, typename R>
 int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
@@ -686,7 +750,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
-            k_lu_diag<T, R><<<nfl, 256, 2 * NB * NB * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
+            k_lu_diag<T, R><<<nfl, 512, 2 * NB * NB * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
                                                                        tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             const int trail = maxm - k0 - 1;  // upper bound of m - t0
@@ -759,7 +823,6 @@ __global__ void __launch_bounds__(kRowsPerCta)
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
                 int *err) {
     extern __shared__ unsigned char smem_raw[];
-    T *yk = reinterpret_cast<T *>(smem_raw);  // nrhs x NB
     const int tid = threadIdx.x;
     // gather: right-hand side of the pivots and the children's updates
     for (int fi = blockIdx.x; fi < nfl; fi += gridDim.x) {
@@ -796,28 +859,15 @@ __global__ void __launch_bounds__(kRowsPerCta)
             const int t0 = k0 + w, rbase = t0 + c * kRowsPerCta;
             if (c > 0 && rbase >= f.m) continue;
             const T *F = pool + f.f_off;
-            const int64_t ld = f.ld;
-            for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-                const int r = idx / w, row = idx % w;
-                const T *wv = W + r * sum_m + f.voff + k0;
-                T acc = wv[row];
-                for (int t = 0; t < row; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], wv[t]);
-                yk[r * NB + row] = acc;
-            }
-            __syncthreads();
+            T *yk = panel_diag_apply<T, R, false>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
+                                                  reinterpret_cast<T *>(smem_raw));
             if (c == 0)
                 for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
                     const int r = idx / w, row = idx % w;
                     Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
                 }
             const int row = rbase + tid;
-            if (row < f.m)
-                for (int r = 0; r < nrhs; ++r) {
-                    T acc = czero<T>();
-                    for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], yk[r * NB + t]);
-                    T &dst = W[r * sum_m + f.voff + row];
-                    dst = csub(dst, acc);
-                }
+            if (row < f.m) panel_row_update(F, f.ld, k0, w, row, yk, nrhs, W + f.voff, sum_m);
             __syncthreads();
         }
         if (!grid_sync(gb, err)) return;
@@ -830,7 +880,7 @@ __global__ void __launch_bounds__(kRowsPerCta)
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
                 T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err) {
     extern __shared__ unsigned char smem_raw[];
-    T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta (also x_k: nrhs x NB)
+    T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
     const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
     const int cch = max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
@@ -888,34 +938,33 @@ __global__ void __launch_bounds__(kRowsPerCta)
             const int rbase = c * kRowsPerCta;
             if (c > 0 && rbase >= k0) continue;
             const T *F = pool + f.f_off;
-            const int64_t ld = f.ld;
-            for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-                const int r = idx / w, row = idx % w;
-                const T *av = W + r * sum_m + f.voff + k0;
-                T acc = czero<T>();
-                for (int t = row; t < w; ++t) cmac(acc, F[(k0 + row) + (int64_t)(k0 + t) * ld], av[t]);
-                xs[r * NB + row] = acc;
-            }
-            __syncthreads();
+            T *xk = panel_diag_apply<T, R, true>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
+                                                 reinterpret_cast<T *>(smem_raw));
             if (c == 0) {
                 const int32_t *v = vars + f.voff + k0;
                 for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
                     const int r = idx / w, row = idx % w;
-                    x[r * n + v[row]] = to_c128(xs[r * NB + row], 1.0);
+                    x[r * n + v[row]] = to_c128(xk[r * NB + row], 1.0);
                 }
             }
             const int row = rbase + tid;
-            if (row < k0)
-                for (int r = 0; r < nrhs; ++r) {
-                    T acc = czero<T>();
-                    for (int t = 0; t < w; ++t) cmac(acc, F[row + (int64_t)(k0 + t) * ld], xs[r * NB + t]);
-                    T &dst = W[r * sum_m + f.voff + row];
-                    dst = csub(dst, acc);
-                }
+            if (row < k0) panel_row_update(F, f.ld, k0, w, row, xk, nrhs, W + f.voff, sum_m);
             __syncthreads();
         }
         if (!grid_sync(gb, err)) return;
     }
+}
+
+template <typename T, typename R>
+int set_smem_attrs() {
+    CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * NB * NB * sizeof(T))));
+    const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    return FDFD_OK;
 }
 
 // x = A^-1 b for nrhs columns (b, x complex128 on device; may alias d_tmp).
@@ -926,9 +975,9 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
     T *W = (T *)fac->d_W, *Y = (T *)fac->d_Y;
     const T *pool = (const T *)fac->d_pool;
     const int64_t sum_m = S.sum_m, n = fac->n;
-    const size_t sm_panel = (size_t)nrhs * NB * sizeof(T);
+    const size_t sm_panel = panel_smem_bytes<T>(nrhs);
     CUDA_TRY(cudaMemsetAsync(fac->d_bar, 0, sizeof(GridBar), st));
-    const size_t sm_coop = (size_t)nrhs * kRowsPerCta * sizeof(T);
+    const size_t sm_coop = std::max(panel_smem_bytes<T>(nrhs), (size_t)nrhs * kRowsPerCta * sizeof(T));
     for (int L = 0; L < S.nlev; ++L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
         prof_begin(PROF_SOLVE_FWD, st);
@@ -939,7 +988,11 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
                             (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err};
-            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(fac->coop_grid),
+            // grid: the most work items any phase of this level has, capped
+            // at the co-resident limit (fewer CTAs make cheaper barriers)
+            const int items = std::max(nfl, nfl * ((maxm + kRowsPerCta - 1) / kRowsPerCta));
+            const int grid = std::max(1, std::min(fac->coop_grid, items));
+            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
@@ -970,7 +1023,11 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
                             (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
                             (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
                             (void *)&gb, (void *)&err};
-            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(fac->coop_grid),
+            const int prw = (maxpp + kRowsPerCta - 1) / kRowsPerCta;
+            const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
+            const int items = std::max(nfl * prw * cch, nfl);
+            const int grid = std::max(1, std::min(fac->coop_grid, items));
+            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
             prof_end(PROF_SOLVE_BWD, st, 1);
             continue;
@@ -1180,7 +1237,7 @@ int coop_grid_for(int max_nrhs, int *grid) {
         *grid = 0;
         return FDFD_OK;
     }
-    const size_t smem = (size_t)max_nrhs * kRowsPerCta * sizeof(T);
+    const size_t smem = std::max(panel_smem_bytes<T>(max_nrhs), (size_t)max_nrhs * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_fwd_level<T, R>, kRowsPerCta, smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_bwd_level<T, R>, kRowsPerCta, smem));
     const int per_sm = std::min(std::min(nb1, nb2), 2);

@@ -205,11 +205,24 @@ __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__
     }
 }
 
-// ---- the GEMM tile ---------------------------------------------------------
+// ---- the GEMM ------------------------------------------------------------------
+// One CTA = one 128-row tile of C and up to kColTilesPerCta 32-column tiles.
+// Warp 4 (lane 0) is the control thread: it pulls the A tile (hi, lo) once,
+// then for each column tile pulls B (hi, lo) into the single B buffer once
+// the previous tile's MMAs have released it, and issues 48 MMAs into one of
+// two TMEM accumulators.  Warps 0-3 drain the other accumulator meanwhile
+// (tcgen05.ld of their 32 TMEM lanes, C -= acc) and hand it back through an
+// mbarrier.  Every wait is bounded.
+constexpr int kColTilesPerCta = 8;
 constexpr uint32_t kSmemBytes = 2 * kATileBytes + 2 * kBTileBytes + 256;
 constexpr uint32_t kWaitLimit = 1u << 22;
+constexpr int kCtaThreads = 160;
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kCtaThreads, 1)
     k_schur_tc(const TcFront *__restrict__ fr, c64 *pool, int f_begin, int k0, const uint8_t *scratch,
                int *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -217,22 +230,30 @@ __global__ void __launch_bounds__(128, 1)
     const int w = min(kPanel, f.p - k0);
     if (w <= 0) return;
     const int t0 = k0 + w, mt = f.m - t0;
-    const int rt = blockIdx.y, ct = blockIdx.z;
-    if (rt * kTileM >= mt || ct * kTileNc >= mt) return;
+    const int rt = blockIdx.y;
+    const int cts = (mt + kTileNc - 1) / kTileNc;
+    const int ct0 = blockIdx.z * kColTilesPerCta;
+    if (rt * kTileM >= mt || ct0 >= cts) return;
+    const int J = min(kColTilesPerCta, cts - ct0);
 
     uint8_t *a_hi = smem, *a_lo = smem + kATileBytes;
     uint8_t *b_hi = smem + 2 * kATileBytes, *b_lo = b_hi + kBTileBytes;
     uint64_t *bars = (uint64_t *)(smem + 2 * kATileBytes + 2 * kBTileBytes);
-    uint32_t *tmem_slot = (uint32_t *)(bars + 2);
+    uint64_t *bar_a = &bars[0], *bar_b = &bars[1], *bar_mma = &bars[2], *bar_epi = &bars[4];
+    uint32_t *tmem_slot = (uint32_t *)(bars + 6);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        mbar_init(bar_a, 1);
+        mbar_init(bar_b, 1);
+        mbar_init(&bar_mma[0], 1);
+        mbar_init(&bar_mma[1], 1);
+        mbar_init(&bar_epi[0], 4);
+        mbar_init(&bar_epi[1], 4);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) {
-        tmem_alloc(tmem_slot, kTmemCols);
+    if (warp == 4) {
+        tmem_alloc(tmem_slot, 2 * kTmemCols);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -240,77 +261,88 @@ __global__ void __launch_bounds__(128, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    bool ok = true;
-    if (threadIdx.x == 0) {
-        const uint8_t *ga = scratch + f.a_off + (size_t)rt * 2 * kATileBytes;
-        const uint8_t *gb = scratch + f.b_off + (size_t)ct * 2 * kBTileBytes;
-        mbar_arrive_expect_tx(&bars[0], 2 * kATileBytes + 2 * kBTileBytes);
-        bulk_g2s(a_hi, ga, kATileBytes, &bars[0]);
-        bulk_g2s(a_lo, ga + kATileBytes, kATileBytes, &bars[0]);
-        bulk_g2s(b_hi, gb, kBTileBytes, &bars[0]);
-        bulk_g2s(b_lo, gb + kBTileBytes, kBTileBytes, &bars[0]);
-        ok = mbar_wait_bounded(&bars[0], 0, kWaitLimit);
-        if (ok) {
-            tc_fence_after();
+    if (warp == 4) {
+        if (lane == 0) {
+            bool ok = true;
+            const uint8_t *ga = scratch + f.a_off + (size_t)rt * 2 * kATileBytes;
+            mbar_arrive_expect_tx(bar_a, 2 * kATileBytes);
+            bulk_g2s(a_hi, ga, kATileBytes, bar_a);
+            bulk_g2s(a_lo, ga + kATileBytes, kATileBytes, bar_a);
+            ok = mbar_wait_bounded(bar_a, 0, kWaitLimit);
             constexpr uint32_t idesc = idesc_tf32(kTileM, 2 * kTileNc);
-            constexpr uint32_t a_step = 2 * (kTileM / 8) * 128;       // bytes per K-step
+            constexpr uint32_t a_step = 2 * (kTileM / 8) * 128;
             constexpr uint32_t b_step = 2 * (2 * kTileNc / 8) * 128;
             const uint32_t sa_hi = smem_u32(a_hi), sa_lo = smem_u32(a_lo);
             const uint32_t sb_hi = smem_u32(b_hi), sb_lo = smem_u32(b_lo);
-            uint32_t acc = 0;
-            for (int s = 0; s < 2 * kPanel / 8; ++s) {
-                const uint64_t ah = smem_desc(sa_hi + s * a_step, (kTileM / 8) * 128, 128);
-                const uint64_t al = smem_desc(sa_lo + s * a_step, (kTileM / 8) * 128, 128);
-                const uint64_t bh = smem_desc(sb_hi + s * b_step, (2 * kTileNc / 8) * 128, 128);
-                const uint64_t bl = smem_desc(sb_lo + s * b_step, (2 * kTileNc / 8) * 128, 128);
-                mma_tf32(tmem, ah, bh, idesc, acc);
-                acc = 1;
-                mma_tf32(tmem, ah, bl, idesc, 1);
-                mma_tf32(tmem, al, bh, idesc, 1);
+            for (int j = 0; j < J && ok; ++j) {
+                const int sidx = j & 1;
+                if (j >= 1 && !mbar_wait_bounded(&bar_mma[(j - 1) & 1], ((j - 1) >> 1) & 1, kWaitLimit)) {
+                    ok = false;  // B buffer still in use
+                    break;
+                }
+                const uint8_t *gb = scratch + f.b_off + (size_t)(ct0 + j) * 2 * kBTileBytes;
+                mbar_arrive_expect_tx(bar_b, 2 * kBTileBytes);
+                bulk_g2s(b_hi, gb, kBTileBytes, bar_b);
+                bulk_g2s(b_lo, gb + kBTileBytes, kBTileBytes, bar_b);
+                if (!mbar_wait_bounded(bar_b, j & 1, kWaitLimit)) { ok = false; break; }
+                if (j >= 2 && !mbar_wait_bounded(&bar_epi[sidx], ((j - 2) >> 1) & 1, kWaitLimit)) {
+                    ok = false;  // accumulator still being drained
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(sidx * kTmemCols);
+                for (int s2 = 0; s2 < 2 * kPanel / 8; ++s2) {
+                    const uint64_t ah = smem_desc(sa_hi + s2 * a_step, (kTileM / 8) * 128, 128);
+                    const uint64_t al = smem_desc(sa_lo + s2 * a_step, (kTileM / 8) * 128, 128);
+                    const uint64_t bh = smem_desc(sb_hi + s2 * b_step, (2 * kTileNc / 8) * 128, 128);
+                    const uint64_t bl = smem_desc(sb_lo + s2 * b_step, (2 * kTileNc / 8) * 128, 128);
+                    mma_tf32(d, ah, bh, idesc, s2 > 0 ? 1u : 0u);
+                    mma_tf32(d, ah, bl, idesc, 1);
+                    mma_tf32(d, al, bh, idesc, 1);
+                }
+                mma_commit(&bar_mma[sidx]);
             }
-            mma_commit(&bars[1]);
-        } else {
-            atomicExch(err, 1);
-            mbar_wait_bounded(&bars[0], 0, kWaitLimit);  // let the copies land
+            if (!ok) atomicExch(err, 1);
         }
-    }
-    // everybody waits for the accumulator (or learns that thread 0 failed)
-    __shared__ int s_ok;
-    if (threadIdx.x == 0) s_ok = ok ? 1 : 0;
-    __syncthreads();
-    bool have_acc = s_ok != 0;
-    if (have_acc && !mbar_wait_bounded(&bars[1], 0, kWaitLimit)) {
-        atomicExch(err, 2);
-        have_acc = false;
-    }
-    tc_fence_after();
-    const int all_acc = __syncthreads_and(have_acc ? 1 : 0);
-    if (s_ok && !all_acc) mbar_wait_bounded(&bars[1], 0, kWaitLimit);  // drain before freeing TMEM
-    if (all_acc) {
-        // warp w owns accumulator rows (TMEM lanes) 32w .. 32w+31
+    } else {
+        // epilogue warps 0-3: warp w owns TMEM lanes (accumulator rows) 32w..32w+31
         const int row = t0 + rt * kTileM + warp * 32 + lane;
         c64 *F = pool + f.f_off;
         const int64_t ld = f.ld;
-        for (int c0 = 0; c0 < 2 * kTileNc; c0 += 16) {
-            uint32_t r[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-            tmem_ld_wait();
-            if (row < f.m) {
+        for (int j = 0; j < J; ++j) {
+            const int sidx = j & 1;
+            const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
+            if (!__all_sync(0xffffffffu, got)) {
+                if (lane == 0) atomicExch(err, 2);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t base = tmem + (uint32_t)(sidx * kTmemCols) + ((uint32_t)(warp * 32) << 16);
+            const int colbase = t0 + (ct0 + j) * kTileNc;
+            for (int c0 = 0; c0 < 2 * kTileNc; c0 += 16) {
+                uint32_t r[16];
+                tmem_ld16(base + (uint32_t)c0, r);
+                tmem_ld_wait();
+                if (row < f.m) {
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int col = t0 + ct * kTileNc + c0 / 2 + q;
-                    if (col < f.m) {
-                        c64 &dst = F[row + (int64_t)col * ld];
-                        dst.x -= __uint_as_float(r[2 * q]);
-                        dst.y -= __uint_as_float(r[2 * q + 1]);
+                    for (int q = 0; q < 8; ++q) {
+                        const int col = colbase + c0 / 2 + q;
+                        if (col < f.m) {
+                            c64 &dst = F[row + (int64_t)col * ld];
+                            dst.x -= __uint_as_float(r[2 * q]);
+                            dst.y -= __uint_as_float(r[2 * q + 1]);
+                        }
                     }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_epi[sidx]);
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+    if (warp == 4) tmem_dealloc(tmem, 2 * kTmemCols);
 }
 
 }  // namespace tc
@@ -323,7 +355,9 @@ int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, in
     if (rts < 1 || cts < 1) return FDFD_OK;
     tc::k_pack_a<<<dim3(nfl, rts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
     tc::k_pack_b<<<dim3(nfl, cts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
-    tc::k_schur_tc<<<dim3(nfl, rts, cts), 128, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, scratch, err);
+    const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
+    tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, scratch,
+                                                                                err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("schur_tc: ") + cudaGetErrorString(e));
     return FDFD_OK;
