@@ -155,8 +155,11 @@ template <typename T, typename R>
 __global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, R tiny,
                           int *tiny_count) {
     extern __shared__ unsigned char smem_raw[];
-    T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major
-    T *X = D + NB * NB;
+    // Padded leading dimension NB + 1: column and row accesses are both free
+    // of shared-memory bank conflicts.
+    constexpr int LS = NB + 1;
+    T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major, ld LS
+    T *X = D + NB * LS;
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
@@ -165,28 +168,28 @@ __global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, i
     const int tid = threadIdx.x;
     for (int idx = tid; idx < w * w; idx += blockDim.x) {
         const int r = idx % w, c = idx / w;
-        D[r + c * NB] = F[r + c * ld];
+        D[r + c * LS] = F[r + c * ld];
     }
     __syncthreads();
     for (int jj = 0; jj < w; ++jj) {
         if (tid == 0) {
-            T pv = D[jj + jj * NB];
+            T pv = D[jj + jj * LS];
             const R a = sqrt(cabs2(pv));
             if (!(a >= tiny)) {
                 // Static pivot: keep the phase, lift the modulus to tiny.
                 pv = (a > R(0)) ? cmake<R>(pv.x / a * tiny, pv.y / a * tiny) : cmake<R>(tiny, R(0));
-                D[jj + jj * NB] = pv;
+                D[jj + jj * LS] = pv;
                 atomicAdd(tiny_count, 1);
             }
         }
         __syncthreads();
-        const T inv = crecip(D[jj + jj * NB]);
-        for (int r = jj + 1 + tid; r < w; r += blockDim.x) D[r + jj * NB] = cmul(D[r + jj * NB], inv);
+        const T inv = crecip(D[jj + jj * LS]);
+        for (int r = jj + 1 + tid; r < w; r += blockDim.x) D[r + jj * LS] = cmul(D[r + jj * LS], inv);
         __syncthreads();
         const int rem = w - jj - 1;
         for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
             const int r = jj + 1 + idx % rem, c = jj + 1 + idx / rem;
-            cmsub(D[r + c * NB], D[r + jj * NB], D[jj + c * NB]);
+            cmsub(D[r + c * LS], D[r + jj * LS], D[jj + c * LS]);
         }
         __syncthreads();
     }
@@ -205,11 +208,11 @@ __global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, i
                 T xt;
                 xt.x = __shfl_sync(0xffffffffu, own.x, t & 31);
                 xt.y = __shfl_sync(0xffffffffu, own.y, t & 31);
-                if (lane > t && lane < w) cmsub(x0, D[lane + t * NB], xt);
-                if (lane + 32 > t && lane + 32 < w) cmsub(x1, D[lane + 32 + t * NB], xt);
+                if (lane > t && lane < w) cmsub(x0, D[lane + t * LS], xt);
+                if (lane + 32 > t && lane + 32 < w) cmsub(x1, D[lane + 32 + t * LS], xt);
             }
-            if (lane > c && lane < w) X[lane + c * NB] = x0;
-            if (lane + 32 > c && lane + 32 < w) X[lane + 32 + c * NB] = x1;
+            if (lane > c && lane < w) X[lane + c * LS] = x0;
+            if (lane + 32 > c && lane + 32 < w) X[lane + 32 + c * LS] = x1;
         } else {
             // row r of inv(U): y U = e_r; for c >= r: y[c] = (e_r[c] - a[c]) / U[c,c],
             // then a[c+1:] += y[c] U[c, c+1:]
@@ -222,22 +225,22 @@ __global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, i
                 if (mine0 || mine1) {
                     const T ac = mine0 ? a0 : a1;
                     const T num = cmake<R>((c == r ? R(1) : R(0)) - ac.x, -ac.y);
-                    yc = cmul(num, crecip(D[c + c * NB]));
+                    yc = cmul(num, crecip(D[c + c * LS]));
                     if (mine0) y0 = yc; else y1 = yc;
                 }
                 yc.x = __shfl_sync(0xffffffffu, yc.x, c & 31);
                 yc.y = __shfl_sync(0xffffffffu, yc.y, c & 31);
-                if (lane > c && lane < w) cmac(a0, yc, D[c + lane * NB]);
-                if (lane + 32 > c && lane + 32 < w) cmac(a1, yc, D[c + (lane + 32) * NB]);
+                if (lane > c && lane < w) cmac(a0, yc, D[c + lane * LS]);
+                if (lane + 32 > c && lane + 32 < w) cmac(a1, yc, D[c + (lane + 32) * LS]);
             }
-            if (lane >= r && lane < w) X[r + lane * NB] = y0;
-            if (lane + 32 >= r && lane + 32 < w) X[r + (lane + 32) * NB] = y1;
+            if (lane >= r && lane < w) X[r + lane * LS] = y0;
+            if (lane + 32 >= r && lane + 32 < w) X[r + (lane + 32) * LS] = y1;
         }
     }
     __syncthreads();
     for (int idx = tid; idx < w * w; idx += blockDim.x) {
         const int r = idx % w, c = idx / w;
-        F[r + c * ld] = X[r + c * NB];
+        F[r + c * ld] = X[r + c * LS];
     }
 }
 
@@ -428,33 +431,88 @@ __device__ __forceinline__ T *panel_diag_apply(const T *F, int64_t ld, int k0, i
     return out;
 }
 
-// dst[row] -= F[row, k0:k0+w] y for one row and all right-hand sides.
+// Row-block update of a panel step: dst[row] -= F[row, k0:k0+w] y for the
+// kItemRows rows starting at rbase (rows >= rend skipped).  Four threads
+// share a row, each with 16 independent column loads in flight, and the
+// four partial sums meet through warp shuffles: the update is bound by how
+// many loads are outstanding, not by arithmetic.
+constexpr int kItemRows = 64;
 template <typename T>
-__device__ __forceinline__ void panel_row_update(const T *F, int64_t ld, int k0, int w, int row, const T *y,
-                                                 int nrhs, T *dst, int64_t dstride) {
+__device__ __forceinline__ void panel_rows_update(const T *F, int64_t ld, int k0, int w, int rbase, int rend,
+                                                  const T *y, int nrhs, T *dst, int64_t dstride) {
+    const int rr = threadIdx.x >> 2, q = threadIdx.x & 3;
+    const int row = rbase + rr;
+    const bool live = row < rend;
     T acc[8];
     for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-    const T *Fr = F + row + (int64_t)k0 * ld;
-    int t = 0;
-    for (; t + 4 <= w; t += 4) {
-        const T a0 = Fr[(int64_t)t * ld], a1 = Fr[(int64_t)(t + 1) * ld];
-        const T a2 = Fr[(int64_t)(t + 2) * ld], a3 = Fr[(int64_t)(t + 3) * ld];
-        for (int r = 0; r < nrhs; ++r) {
-            const T *yr = y + r * NB + t;
-            cmac(acc[r], a0, yr[0]);
-            cmac(acc[r], a1, yr[1]);
-            cmac(acc[r], a2, yr[2]);
-            cmac(acc[r], a3, yr[3]);
+    if (live) {
+        const T *Fr = F + row + (int64_t)(k0 + 16 * q) * ld;
+        const int t0 = 16 * q;
+        if (t0 + 16 <= w) {
+            T a[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) a[i] = Fr[(int64_t)i * ld];
+            for (int r = 0; r < nrhs; ++r) {
+                const T *yr = y + r * NB + t0;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) cmac(acc[r], a[i], yr[i]);
+            }
+        } else {
+            for (int i = 0; t0 + i < w; ++i) {
+                const T a = Fr[(int64_t)i * ld];
+                for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, y[r * NB + t0 + i]);
+            }
         }
     }
-    for (; t < w; ++t) {
-        const T a = Fr[(int64_t)t * ld];
-        for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, y[r * NB + t]);
-    }
     for (int r = 0; r < nrhs; ++r) {
-        T &d = dst[r * dstride + row];
-        d = csub(d, acc[r]);
+        for (int off = 1; off < 4; off <<= 1) {
+            acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, off);
+            acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, off);
+        }
+        if (live && q == 0) {
+            T &d = dst[r * dstride + row];
+            d = csub(d, acc[r]);
+        }
     }
+}
+
+// Row-block product for the backward opener: acc[rhs] = sum over columns
+// [c0, c0+cn) of F[row, c] xs[rhs][c - c0] (xs in shared memory, row
+// stride kRowsPerCta), four threads per row as in panel_rows_update.
+template <typename T>
+__device__ __forceinline__ void opener_rows_product(const T *F, int64_t ld, int row, bool live, int c0, int cn,
+                                                    const T *xs, int nrhs, T (&acc)[8]) {
+    const int q = threadIdx.x & 3;
+    if (live) {
+        for (int cb = 16 * q; cb < cn; cb += 64) {
+            const T *Fr = F + row + (int64_t)(c0 + cb) * ld;
+            const int len = min(16, cn - cb);
+            if (len == 16) {
+                T a[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) a[i] = Fr[(int64_t)i * ld];
+                for (int r = 0; r < nrhs; ++r) {
+                    const T *xr = xs + r * kRowsPerCta + cb;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) cmac(acc[r], a[i], xr[i]);
+                }
+            } else {
+                for (int i = 0; i < len; ++i) {
+                    const T a = Fr[(int64_t)i * ld];
+                    for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, xs[r * kRowsPerCta + cb + i]);
+                }
+            }
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void quad_reduce(T (&acc)[8], int nrhs) {
+    for (int r = 0; r < nrhs; ++r)
+        for (int off = 1; off < 4; off <<= 1) {
+            acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, off);
+            acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, off);
+        }
 }
 
 // Forward, one panel: y_k = inv(L_kk) w_k (every CTA of the front computes
@@ -467,7 +525,7 @@ __global__ void k_fwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
     const int t0 = k0 + w;
-    const int rbase = t0 + blockIdx.y * kRowsPerCta;
+    const int rbase = t0 + blockIdx.y * kItemRows;
     if (blockIdx.y > 0 && rbase >= f.m) return;
     const T *F = pool + f.f_off;
     const int tid = threadIdx.x;
@@ -478,8 +536,7 @@ __global__ void k_fwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
             const int r = idx / w, row = idx % w;
             Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
         }
-    const int row = rbase + tid;
-    if (row < f.m) panel_row_update(F, f.ld, k0, w, row, yk, nrhs, W + f.voff, sum_m);
+    panel_rows_update(F, f.ld, k0, w, rbase, f.m, yk, nrhs, W + f.voff, sum_m);
 }
 
 // Backward, step 1: acc[0:p] = y[0:p] - U[0:p, p:m] x_B, x_B read from the
@@ -492,14 +549,13 @@ __global__ void k_bwd_init(const FrontD *__restrict__ fr, const T *__restrict__ 
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta
     const FrontD f = fr[f_begin + blockIdx.x];
-    const int row = blockIdx.y * kRowsPerCta + threadIdx.x;
-    if (blockIdx.y * kRowsPerCta >= f.p) return;
-    const T *F = pool + f.f_off;
-    const int64_t ld = f.ld;
+    const int rbase = blockIdx.y * kItemRows;
+    if (rbase >= f.p) return;
+    const int row = rbase + (threadIdx.x >> 2);
+    const bool live = row < f.p;
     const int32_t *v = vars + f.voff;
     T acc[8];
-    for (int r = 0; r < nrhs; ++r)
-        acc[r] = (row < f.p) ? Y[r * sum_m + f.voff + row] : czero<T>();
+    for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
     for (int c0 = f.p; c0 < f.m; c0 += kRowsPerCta) {
         const int cn = min(kRowsPerCta, f.m - c0);
         __syncthreads();
@@ -508,14 +564,11 @@ __global__ void k_bwd_init(const FrontD *__restrict__ fr, const T *__restrict__ 
             xs[r * kRowsPerCta + cc] = from_c128<T>(x[r * n + v[c0 + cc]], s_in[r]);
         }
         __syncthreads();
-        if (row < f.p)
-            for (int cc = 0; cc < cn; ++cc) {
-                const T a = F[row + (int64_t)(c0 + cc) * ld];
-                for (int r = 0; r < nrhs; ++r) cmsub(acc[r], a, xs[r * kRowsPerCta + cc]);
-            }
+        opener_rows_product(pool + f.f_off, (int64_t)f.ld, row, live, c0, cn, xs, nrhs, acc);
     }
-    if (row < f.p)
-        for (int r = 0; r < nrhs; ++r) W[r * sum_m + f.voff + row] = acc[r];
+    quad_reduce(acc, nrhs);
+    if (live && (threadIdx.x & 3) == 0)
+        for (int r = 0; r < nrhs; ++r) W[r * sum_m + f.voff + row] = csub(Y[r * sum_m + f.voff + row], acc[r]);
     (void)max_nrhs;
 }
 
@@ -533,28 +586,25 @@ __global__ void k_bwd_partial(const FrontD *__restrict__ fr, const T *__restrict
     T *xs = reinterpret_cast<T *>(smem_raw);  // nrhs x kRowsPerCta
     const int fi = f_begin + blockIdx.x;
     const FrontD f = fr[fi];
-    const int rbase = blockIdx.y * kRowsPerCta, c0 = f.p + blockIdx.z * kRowsPerCta;
+    const int rbase = blockIdx.y * kItemRows, c0 = f.p + blockIdx.z * kRowsPerCta;
     if (rbase >= f.p || c0 >= f.m) return;
     const int cn = min(kRowsPerCta, f.m - c0);
     const int32_t *v = vars + f.voff;
     for (int idx = threadIdx.x; idx < cn * nrhs; idx += blockDim.x) {
         const int r = idx / cn, cc = idx % cn;
-        const double2 xv = x[r * n + v[c0 + cc]];
-        xs[r * kRowsPerCta + cc] = from_c128<T>(xv, 1.0);
+        xs[r * kRowsPerCta + cc] = from_c128<T>(x[r * n + v[c0 + cc]], 1.0);
     }
     __syncthreads();
-    const int row = rbase + threadIdx.x;
-    if (row >= f.p) return;
-    const T *F = pool + f.f_off;
-    const int64_t ld = f.ld;
+    const int row = rbase + (threadIdx.x >> 2);
+    const bool live = row < f.p;
     T acc[8];
     for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-    for (int cc = 0; cc < cn; ++cc) {
-        const T a = F[row + (int64_t)(c0 + cc) * ld];
-        for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, xs[r * kRowsPerCta + cc]);
+    opener_rows_product(pool + f.f_off, (int64_t)f.ld, row, live, c0, cn, xs, nrhs, acc);
+    quad_reduce(acc, nrhs);
+    if (live && (threadIdx.x & 3) == 0) {
+        T *out = scratch + bwd_off[fi] + ((int64_t)blockIdx.z * nrhs) * f.p;
+        for (int r = 0; r < nrhs; ++r) out[(int64_t)r * f.p + row] = acc[r];
     }
-    T *out = scratch + bwd_off[fi] + ((int64_t)blockIdx.z * nrhs) * f.p;
-    for (int r = 0; r < nrhs; ++r) out[(int64_t)r * f.p + row] = acc[r];
 }
 
 template <typename T>
@@ -585,7 +635,7 @@ __global__ void k_bwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
-    const int rbase = blockIdx.y * kRowsPerCta;
+    const int rbase = blockIdx.y * kItemRows;
     if (blockIdx.y > 0 && rbase >= k0) return;
     const T *F = pool + f.f_off;
     const int tid = threadIdx.x;
@@ -598,8 +648,7 @@ __global__ void k_bwd_panel(const FrontD *__restrict__ fr, const T *__restrict__
             x[r * n + v[row]] = to_c128(xk[r * NB + row], s_out[r]);
         }
     }
-    const int row = rbase + tid;
-    if (row < k0) panel_row_update(F, f.ld, k0, w, row, xk, nrhs, W + f.voff, sum_m);
+    panel_rows_update(F, f.ld, k0, w, rbase, k0, xk, nrhs, W + f.voff, sum_m);
 }
 
 // Per-column solve scales: s_in = 1/||r||, s_out = sigma ||r||.
@@ -750,8 +799,8 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
-            k_lu_diag<T, R><<<nfl, 512, 2 * NB * NB * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
-                                                                       tiny, fac->d_tiny);
+            k_lu_diag<T, R><<<nfl, 256, 2 * NB * (NB + 1) * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
+                                                                             tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             const int trail = maxm - k0 - 1;  // upper bound of m - t0
             if (trail <= 0) continue;
@@ -850,13 +899,13 @@ __global__ void __launch_bounds__(kRowsPerCta)
     }
     if (!grid_sync(gb, err)) return;
     for (int k0 = 0; k0 < maxp; k0 += NB) {
-        const int maxch = max(1, (maxm - k0 + kRowsPerCta - 1) / kRowsPerCta);
+        const int maxch = max(1, (maxm - k0 + kItemRows - 1) / kItemRows);
         for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
             const int fi = item / maxch, c = item % maxch;
             const FrontD f = fr[fb + fi];
             const int w = min(NB, f.p - k0);
             if (w <= 0) continue;
-            const int t0 = k0 + w, rbase = t0 + c * kRowsPerCta;
+            const int t0 = k0 + w, rbase = t0 + c * kItemRows;
             if (c > 0 && rbase >= f.m) continue;
             const T *F = pool + f.f_off;
             T *yk = panel_diag_apply<T, R, false>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
@@ -866,8 +915,7 @@ __global__ void __launch_bounds__(kRowsPerCta)
                     const int r = idx / w, row = idx % w;
                     Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
                 }
-            const int row = rbase + tid;
-            if (row < f.m) panel_row_update(F, f.ld, k0, w, row, yk, nrhs, W + f.voff, sum_m);
+            panel_rows_update(F, f.ld, k0, w, rbase, f.m, yk, nrhs, W + f.voff, sum_m);
             __syncthreads();
         }
         if (!grid_sync(gb, err)) return;
@@ -882,13 +930,13 @@ __global__ void __launch_bounds__(kRowsPerCta)
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
-    const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
+    const int prow = (maxp + kItemRows - 1) / kItemRows;
     const int cch = max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
-    // opener, pass 1: partial products U[rows, cols] x_B[cols] per 256 x 256 block
+    // opener, pass 1: partial products U[rows, cols] x_B[cols] per 64 x 256 block
     for (int item = blockIdx.x; item < nfl * prow * cch; item += gridDim.x) {
         const int fi = item / (prow * cch), rc = (item / cch) % prow, cc = item % cch;
         const FrontD f = fr[fb + fi];
-        const int rbase = rc * kRowsPerCta, c0 = f.p + cc * kRowsPerCta;
+        const int rbase = rc * kItemRows, c0 = f.p + cc * kRowsPerCta;
         if (rbase >= f.p || c0 >= f.m) continue;
         const int cn = min(kRowsPerCta, f.m - c0);
         const int32_t *v = vars + f.voff;
@@ -897,15 +945,13 @@ __global__ void __launch_bounds__(kRowsPerCta)
             xs[r * kRowsPerCta + q] = from_c128<T>(x[r * n + v[c0 + q]], 1.0);
         }
         __syncthreads();
-        const int row = rbase + tid;
-        if (row < f.p) {
-            const T *F = pool + f.f_off;
-            T acc[8];
-            for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-            for (int q = 0; q < cn; ++q) {
-                const T a = F[row + (int64_t)(c0 + q) * f.ld];
-                for (int r = 0; r < nrhs; ++r) cmac(acc[r], a, xs[r * kRowsPerCta + q]);
-            }
+        const int row = rbase + (tid >> 2);
+        const bool live = row < f.p;
+        T acc[8];
+        for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+        opener_rows_product(pool + f.f_off, (int64_t)f.ld, row, live, c0, cn, xs, nrhs, acc);
+        quad_reduce(acc, nrhs);
+        if (live && (tid & 3) == 0) {
             T *out = scratch + bwd_off[fb + fi] + ((int64_t)cc * nrhs) * f.p;
             for (int r = 0; r < nrhs; ++r) out[(int64_t)r * f.p + row] = acc[r];
         }
@@ -913,8 +959,9 @@ __global__ void __launch_bounds__(kRowsPerCta)
     }
     if (!grid_sync(gb, err)) return;
     // opener, pass 2: acc = y - sum of the column blocks, in a fixed order
-    for (int item = blockIdx.x; item < nfl * prow; item += gridDim.x) {
-        const int fi = item / prow, rc = item % prow;
+    const int prow2 = (maxp + kRowsPerCta - 1) / kRowsPerCta;
+    for (int item = blockIdx.x; item < nfl * prow2; item += gridDim.x) {
+        const int fi = item / prow2, rc = item % prow2;
         const FrontD f = fr[fb + fi];
         const int row = rc * kRowsPerCta + tid;
         if (row < f.p) {
@@ -929,13 +976,13 @@ __global__ void __launch_bounds__(kRowsPerCta)
     }
     if (!grid_sync(gb, err)) return;
     for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
-        const int maxch = max(1, (k0 + kRowsPerCta - 1) / kRowsPerCta);
+        const int maxch = max(1, (k0 + kItemRows - 1) / kItemRows);
         for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
             const int fi = item / maxch, c = item % maxch;
             const FrontD f = fr[fb + fi];
             const int w = min(NB, f.p - k0);
             if (w <= 0) continue;
-            const int rbase = c * kRowsPerCta;
+            const int rbase = c * kItemRows;
             if (c > 0 && rbase >= k0) continue;
             const T *F = pool + f.f_off;
             T *xk = panel_diag_apply<T, R, true>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
@@ -947,8 +994,7 @@ __global__ void __launch_bounds__(kRowsPerCta)
                     x[r * n + v[row]] = to_c128(xk[r * NB + row], 1.0);
                 }
             }
-            const int row = rbase + tid;
-            if (row < k0) panel_row_update(F, f.ld, k0, w, row, xk, nrhs, W + f.voff, sum_m);
+            panel_rows_update(F, f.ld, k0, w, rbase, k0, xk, nrhs, W + f.voff, sum_m);
             __syncthreads();
         }
         if (!grid_sync(gb, err)) return;
@@ -958,7 +1004,7 @@ __global__ void __launch_bounds__(kRowsPerCta)
 template <typename T, typename R>
 int set_smem_attrs() {
     CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(2 * NB * NB * sizeof(T))));
+                                  (int)(2 * NB * (NB + 1) * sizeof(T))));
     const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
@@ -990,7 +1036,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
                             (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err};
             // grid: the most work items any phase of this level has, capped
             // at the co-resident limit (fewer CTAs make cheaper barriers)
-            const int items = std::max(nfl, nfl * ((maxm + kRowsPerCta - 1) / kRowsPerCta));
+            const int items = std::max(nfl, nfl * ((maxm + kItemRows - 1) / kItemRows));
             const int grid = std::max(1, std::min(fac->coop_grid, items));
             CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
@@ -1002,7 +1048,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         int nl = 1;
         for (int k0 = 0; k0 < maxp; k0 += NB, ++nl) {
-            const int rows = std::max(1, (maxm - k0 + kRowsPerCta - 1) / kRowsPerCta);
+            const int rows = std::max(1, (maxm - k0 + kItemRows - 1) / kItemRows);
             k_fwd_panel<T, R><<<dim3(nfl, rows), kRowsPerCta, sm_panel, st>>>(fac->d_fronts, pool, W, Y,
                                                                             sum_m, nrhs, fb, k0);
         }
@@ -1011,7 +1057,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
     for (int L = S.nlev - 1; L >= 0; --L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
         const int maxp = S.lev_max_p[L];
-        const int prow = (maxp + kRowsPerCta - 1) / kRowsPerCta;
+        const int prow = (maxp + kItemRows - 1) / kItemRows;
         prof_begin(PROF_SOLVE_BWD, st);
         if (fac->coop_level[L]) {
             int maxpp = maxp, maxb = 0;
@@ -1023,7 +1069,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
                             (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
                             (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
                             (void *)&gb, (void *)&err};
-            const int prw = (maxpp + kRowsPerCta - 1) / kRowsPerCta;
+            const int prw = (maxpp + kItemRows - 1) / kItemRows;
             const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
             const int items = std::max(nfl * prw * cch, nfl);
             const int grid = std::max(1, std::min(fac->coop_grid, items));
@@ -1040,7 +1086,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             k_bwd_partial<T><<<dim3(nfl, prow, cch), kRowsPerCta, (size_t)nrhs * kRowsPerCta * sizeof(T),
                                st>>>(fac->d_fronts, pool, fac->d_vars, x, fac->d_bwd_off, (T *)fac->d_bwd_scratch,
                                      n, nrhs, fb);
-            k_bwd_reduce<T><<<dim3(nfl, prow), kRowsPerCta, 0, st>>>(fac->d_fronts, fac->d_bwd_off,
+            k_bwd_reduce<T><<<dim3(nfl, (maxp + kRowsPerCta - 1) / kRowsPerCta), kRowsPerCta, 0, st>>>(fac->d_fronts, fac->d_bwd_off,
                                                                     (const T *)fac->d_bwd_scratch, W, Y, sum_m,
                                                                     nrhs, fb);
             nbl = 2;
@@ -1050,7 +1096,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         }
         int nl = nbl;
         for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB, ++nl) {
-            const int rows = std::max(1, (k0 + kRowsPerCta - 1) / kRowsPerCta);
+            const int rows = std::max(1, (k0 + kItemRows - 1) / kItemRows);
             k_bwd_panel<T, R><<<dim3(nfl, rows), kRowsPerCta, sm_panel, st>>>(
                 fac->d_fronts, pool, fac->d_vars, W, x, fac->d_unit, sum_m, n, nrhs, fb, k0);
         }

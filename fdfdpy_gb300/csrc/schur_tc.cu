@@ -311,6 +311,15 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
         const int64_t ld = f.ld;
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
+            const int colbase = t0 + (ct0 + j) * kTileNc;
+            // prefetch this row's 32 C entries of the tile while the MMAs run
+            c64 cv[kTileNc];
+            const bool live = row < f.m;
+#pragma unroll
+            for (int q = 0; q < kTileNc; ++q) {
+                const int col = colbase + q;
+                cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+            }
             const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
             if (!__all_sync(0xffffffffu, got)) {
                 if (lane == 0) atomicExch(err, 2);
@@ -318,21 +327,22 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
             }
             tc_fence_after();
             const uint32_t base = tmem + (uint32_t)(sidx * kTmemCols) + ((uint32_t)(warp * 32) << 16);
-            const int colbase = t0 + (ct0 + j) * kTileNc;
+#pragma unroll
             for (int c0 = 0; c0 < 2 * kTileNc; c0 += 16) {
                 uint32_t r[16];
                 tmem_ld16(base + (uint32_t)c0, r);
                 tmem_ld_wait();
-                if (row < f.m) {
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const int col = colbase + c0 / 2 + q;
-                        if (col < f.m) {
-                            c64 &dst = F[row + (int64_t)col * ld];
-                            dst.x -= __uint_as_float(r[2 * q]);
-                            dst.y -= __uint_as_float(r[2 * q + 1]);
-                        }
-                    }
+                for (int q = 0; q < 8; ++q) {
+                    cv[c0 / 2 + q].x -= __uint_as_float(r[2 * q]);
+                    cv[c0 / 2 + q].y -= __uint_as_float(r[2 * q + 1]);
+                }
+            }
+            if (live) {
+#pragma unroll
+                for (int q = 0; q < kTileNc; ++q) {
+                    const int col = colbase + q;
+                    if (col < f.m) F[row + (int64_t)col * ld] = cv[q];
                 }
             }
             tc_fence_before();
