@@ -87,6 +87,7 @@ SIGNATURES = {
     "fdfd_factor_numeric": (C.c_int, [P, POP, P]),
     "fdfd_factor_solve": (C.c_int, [P, P, P, I32, I32, P]),
     "fdfd_solve_refined": (C.c_int, [P, POP, P, P, I32, I32, D, I32, P]),
+    "fdfd_solve_gmres": (C.c_int, [P, POP, P, P, I32, D, I32, I32, P]),
     "fdfd_factor_stats_get": (C.c_int, [P, C.POINTER(FactorStats)]),
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
     "fdfd_factor_destroy": (None, [P]),

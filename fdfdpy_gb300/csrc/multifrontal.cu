@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -53,6 +54,7 @@ constexpr int BM = 64;        // GEMM tile rows
 constexpr int BN = 64;        // GEMM tile cols
 constexpr int BK = 16;        // GEMM K chunk
 constexpr int kRowsPerCta = 256;
+constexpr int kDotParts = 152 * 2;  // partial sums per GMRES dot product
 
 struct FrontD {
     int64_t f_off;  // element offset of the dense block in the pool
@@ -688,6 +690,76 @@ __global__ void k_pscale(const double2 *in, double2 *out, const double2 *isxf, c
     }
 }
 
+// ---- GMRES building blocks (FP64, one right-hand side) ----------------------
+// Partial dot products h_i = sum conj(V_i) w over a block of the vector for
+// i < nv; partial[i * gridDim.x + block].
+__global__ void k_multidot_partial(const double2 *__restrict__ V, int64_t n, int nv,
+                                   const double2 *__restrict__ w, double2 *partial) {
+    __shared__ double2 red[8];
+    const int i = blockIdx.y;
+    const double2 *vi = V + (size_t)i * n;
+    double sr = 0.0, si = 0.0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const double2 a = vi[k], b = w[k];
+        sr = fma(a.x, b.x, fma(a.y, b.y, sr));   // conj(a) * b
+        si = fma(a.x, b.y, fma(-a.y, b.x, si));
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        sr += __shfl_down_sync(0xffffffffu, sr, off);
+        si += __shfl_down_sync(0xffffffffu, si, off);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(sr, si);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { t.x += red[q].x; t.y += red[q].y; }
+        partial[(size_t)i * gridDim.x + blockIdx.x] = t;
+    }
+    (void)nv;
+}
+__global__ void k_multidot_final(const double2 *partial, int nparts, double2 *out) {
+    __shared__ double2 red[8];
+    const int i = blockIdx.x;
+    double sr = 0.0, si = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
+        sr += partial[(size_t)i * nparts + b].x;
+        si += partial[(size_t)i * nparts + b].y;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        sr += __shfl_down_sync(0xffffffffu, sr, off);
+        si += __shfl_down_sync(0xffffffffu, si, off);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = make_double2(sr, si);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { t.x += red[q].x; t.y += red[q].y; }
+        out[i] = t;
+    }
+}
+// w += sum_i coef_i V_i  (coef on the device, nv <= 32)
+__global__ void k_multiaxpy(double2 *w, const double2 *__restrict__ V, int64_t n, int nv,
+                           const double2 *__restrict__ coef, double sign) {
+    __shared__ double2 c[32];
+    if (threadIdx.x < nv) c[threadIdx.x] = coef[threadIdx.x];
+    __syncthreads();
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        double2 acc = w[k];
+        for (int i = 0; i < nv; ++i) {
+            const double2 v = V[(size_t)i * n + k], a = c[i];
+            acc.x = fma(sign * a.x, v.x, fma(-sign * a.y, v.y, acc.x));
+            acc.y = fma(sign * a.x, v.y, fma(sign * a.y, v.x, acc.y));
+        }
+        w[k] = acc;
+    }
+}
+__global__ void k_scale_copy(const double2 *__restrict__ in, double2 *out, int64_t n, double s) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const double2 a = in[k];
+        out[k] = make_double2(a.x * s, a.y * s);
+    }
+}
+
 __global__ void k_axpy(double2 *x, const double2 *d, int64_t len) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < len;
          k += (int64_t)gridDim.x * blockDim.x) {
@@ -749,6 +821,8 @@ struct fdfd_factor {
     TcFront *d_tcf = nullptr;
     uint8_t *d_scratch = nullptr;
     int *d_tcerr = nullptr;
+    void *d_krylov = nullptr;
+    int krylov_m = 0;
     bool numeric_done = false;
     bool has_p = false;  // PML factors known: transposed solves allowed
     int Nx = 0, Ny = 0;
@@ -1167,7 +1241,7 @@ void free_factor(fdfd_factor *f) {
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
                     f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
-                    f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch};
+                    f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch, f->d_krylov};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -1535,6 +1609,144 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
         return fail(FDFD_ERR_NOT_CONVERGED, "solve_refined: residual " + std::to_string(worst) +
                                                 " above tolerance after " + std::to_string(it) +
                                                 " refinement steps");
+    return FDFD_OK;
+}
+
+// Right-preconditioned restarted GMRES in FP64 with the factor as the
+// preconditioner M ~ A: x = x0 + M^-1 V y.  Arnoldi with two passes of
+// classical Gram-Schmidt (batched dot products, one host round trip per
+// pass), Givens rotations on the host.  Refinement by GMRES converges in
+// fewer factor applications than plain refinement when the factor is only
+// FP32 accurate.
+extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const void *b, void *x,
+                                int32_t transpose, double tol, int32_t max_iter, int32_t restart,
+                                void *stream) {
+    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: NULL argument");
+    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: factor has no numeric values");
+    if (restart < 1 || restart > 30 || max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: restart must be 1..30");
+    OpDev o;
+    int rc = make_opdev(op, &o);
+    if (rc) return rc;
+    if (op->Nx != fac->Nx || op->Ny != fac->Ny)
+        return fail(FDFD_ERR_BAD_ARG, "solve_gmres: operator grid differs from the factor grid");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n = fac->n;
+    const int m = restart;
+    const int mode_apply = transpose ? 2 : 1, mode_res = transpose ? 3 : 0;
+    const double2 *bb = (const double2 *)b;
+    double2 *xx = (double2 *)x;
+    // workspace: V (m+1 vectors), Z (m vectors), w; partial sums; coefficients
+    if (!fac->d_krylov || fac->krylov_m < m) {
+        if (fac->d_krylov) cudaFree(fac->d_krylov);
+        fac->d_krylov = nullptr;
+        const size_t bytes = (size_t)(2 * m + 2) * n * sizeof(double2) + (size_t)(m + 2) * kDotParts * sizeof(double2) +
+                             64 * sizeof(double2);
+        if (cudaMalloc(&fac->d_krylov, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(FDFD_ERR_OOM, "solve_gmres: Krylov workspace allocation failed");
+        }
+        fac->krylov_m = m;
+    }
+    double2 *V = (double2 *)fac->d_krylov;
+    double2 *Z = V + (size_t)(m + 1) * n;
+    double2 *w = Z + (size_t)m * n;
+    double2 *partial = w + n;
+    double2 *coef = partial + (size_t)(m + 2) * kDotParts;
+    std::vector<double2> hcoef(m + 2);
+    CUDA_TRY(cudaEventRecord(fac->ev[2], st));
+    CUDA_TRY(cudaMemsetAsync(fac->d_solve_err, 0, sizeof(int), st));
+    auto dots = [&](int nv, const double2 *vec) -> int {  // hcoef[0:nv] = V[0:nv]^H vec
+        k_multidot_partial<<<dim3(kDotParts, nv), 256, 0, st>>>(V, n, nv, vec, partial);
+        k_multidot_final<<<nv, 256, 0, st>>>(partial, kDotParts, coef);
+        CUDA_TRY(cudaMemcpyAsync(hcoef.data(), coef, nv * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        return FDFD_OK;
+    };
+    auto norm_of = [&](const double2 *vec, double *out) -> int {
+        int r2 = norms_device(vec, n, 1, fac->d_partial, fac->d_norm, st);
+        if (r2) return r2;
+        CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        *out = fac->h_norm[0];
+        return FDFD_OK;
+    };
+    double bnorm = 0.0;
+    if ((rc = norm_of(bb, &bnorm))) return rc;
+    if (bnorm == 0.0) {
+        CUDA_TRY(cudaMemsetAsync(xx, 0, n * sizeof(double2), st));
+        fac->stats.refine_iters = 0;
+        fac->stats.rel_residual = 0.0;
+        return FDFD_OK;
+    }
+    // x0 = M^-1 b
+    if ((rc = apply_factor(fac, bb, xx, 1, transpose, st))) return rc;
+    int apps = 1;
+    double rel = 0.0;
+    std::vector<std::complex<double>> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1);
+    for (;;) {
+        // r = b - A x into V[0]
+        if ((rc = apply_device(o, xx, bb, V, 1, mode_res, st))) return rc;
+        double beta = 0.0;
+        if ((rc = norm_of(V, &beta))) return rc;
+        rel = beta / bnorm;
+        if (!(rel > tol) || apps > max_iter) break;
+        k_scale_copy<<<grid1(n), 256, 0, st>>>(V, V, n, 1.0 / beta);
+        std::fill(g.begin(), g.end(), std::complex<double>(0.0));
+        g[0] = beta;
+        int j = 0;
+        for (; j < m && apps <= max_iter; ++j) {
+            double2 *vj = V + (size_t)j * n, *zj = Z + (size_t)j * n;
+            if ((rc = apply_factor(fac, vj, zj, 1, transpose, st))) return rc;
+            ++apps;
+            if ((rc = apply_device(o, zj, nullptr, w, 1, mode_apply, st))) return rc;
+            for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = 0.0;
+            for (int pass = 0; pass < 2; ++pass) {   // CGS2
+                if ((rc = dots(j + 1, w))) return rc;
+                for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] += std::complex<double>(hcoef[i].x, hcoef[i].y);
+                k_multiaxpy<<<grid1(n), 256, 0, st>>>(w, V, n, j + 1, coef, -1.0);
+            }
+            double hn = 0.0;
+            if ((rc = norm_of(w, &hn))) return rc;
+            H[(size_t)(j + 1) * m + j] = hn;
+            if (hn > 0.0) k_scale_copy<<<grid1(n), 256, 0, st>>>(w, V + (size_t)(j + 1) * n, n, 1.0 / hn);
+            // Givens rotations
+            for (int i = 0; i < j; ++i) {
+                const std::complex<double> a = H[(size_t)i * m + j], bq = H[(size_t)(i + 1) * m + j];
+                H[(size_t)i * m + j] = std::conj(cs[i]) * a + std::conj(sn[i]) * bq;
+                H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * bq;
+            }
+            const std::complex<double> a = H[(size_t)j * m + j], bq = H[(size_t)(j + 1) * m + j];
+            const double den = std::sqrt(std::norm(a) + std::norm(bq));
+            cs[j] = den > 0 ? a / den : 1.0;
+            sn[j] = den > 0 ? bq / den : 0.0;
+            H[(size_t)j * m + j] = den;
+            H[(size_t)(j + 1) * m + j] = 0.0;
+            g[j + 1] = -sn[j] * g[j];
+            g[j] = std::conj(cs[j]) * g[j];
+            if (std::abs(g[j + 1]) / bnorm <= 0.5 * tol || hn == 0.0) { ++j; break; }
+        }
+        // y = H^-1 g (upper triangular j x j); x += Z y
+        std::vector<std::complex<double>> y(j);
+        for (int i = j - 1; i >= 0; --i) {
+            std::complex<double> t = g[i];
+            for (int k = i + 1; k < j; ++k) t -= H[(size_t)i * m + k] * y[k];
+            y[i] = t / H[(size_t)i * m + i];
+        }
+        for (int i = 0; i < j; ++i) hcoef[i] = make_double2(y[i].real(), y[i].imag());
+        CUDA_TRY(cudaMemcpyAsync(coef, hcoef.data(), j * sizeof(double2), cudaMemcpyHostToDevice, st));
+        double2 *Zb = Z;
+        k_multiaxpy<<<grid1(n), 256, 0, st>>>(xx, Zb, n, j, coef, 1.0);
+        CUDA_TRY(cudaGetLastError());
+    }
+    CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (*fac->h_err) return fail(FDFD_ERR_CUDA, "solve_gmres: a grid barrier of the cooperative solve timed out");
+    CUDA_TRY(cudaEventRecord(fac->ev[3], st));
+    fac->stats.refine_iters = apps - 1;
+    fac->stats.rel_residual = rel;
+    if (!(rel <= tol))
+        return fail(FDFD_ERR_NOT_CONVERGED, "solve_gmres: residual " + std::to_string(rel) + " above tolerance after " +
+                                                std::to_string(apps) + " factor applications");
     return FDFD_OK;
 }
 

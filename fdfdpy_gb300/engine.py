@@ -279,17 +279,25 @@ class Factor:
         return torch.cat(outs).reshape(b.shape)
 
     def solve(self, b, transpose=False, tol=1e-12, max_iter=10, op: DeviceOperator | None = None,
-              raise_on_fail=False):
-        """x with ||b - A x|| <= tol ||b|| per column (FP64 refinement)."""
+              raise_on_fail=False, method="ir", restart=20):
+        """x with ||b - A x|| <= tol ||b|| per column: FP64 iterative
+        refinement (method='ir') or factor-preconditioned GMRES
+        (method='gmres', one column at a time)."""
         op = self.op if op is None else op
         b = as_c128(b)
         n = op.n
         s = op.struct()
         outs, worst, iters = [], 0.0, 0
-        for blk in self._chunks(b, n):
+        blocks = self._chunks(b, n) if method == "ir" else (col.contiguous() for col in b.reshape(-1, n))
+        for blk in blocks:
             x = torch.empty_like(blk)
-            code = N.lib().fdfd_solve_refined(self.handle, C.byref(s), _ptr(blk), _ptr(x), blk.shape[0],
-                                              int(bool(transpose)), float(tol), int(max_iter), stream_ptr())
+            if method == "gmres":
+                code = N.lib().fdfd_solve_gmres(self.handle, C.byref(s), _ptr(blk), _ptr(x), int(bool(transpose)),
+                                                float(tol), int(max_iter), int(restart), stream_ptr())
+            else:
+                code = N.lib().fdfd_solve_refined(self.handle, C.byref(s), _ptr(blk), _ptr(x),
+                                                  blk.reshape(-1, n).shape[0], int(bool(transpose)), float(tol),
+                                                  int(max_iter), stream_ptr())
             if code != N.FDFD_ERR_NOT_CONVERGED or raise_on_fail:
                 N.check(code, "fdfd_solve_refined")
             st = self.stats()

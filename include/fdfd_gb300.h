@@ -243,6 +243,15 @@ int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
  * sqrt(eps) = 1.5e-8 for complex128).  Takes effect at the next
  * fdfd_factor_numeric.                                                   */
 int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol);
+/* One right-hand side by restarted GMRES(restart) in FP64, right-
+ * preconditioned by the factor; stops at ||b - A x|| <= tol ||b|| or after
+ * max_iter factor applications (FDFD_ERR_NOT_CONVERGED, x still written).
+ * Same result contract as fdfd_solve_refined, usually with fewer factor
+ * applications for a complex64 factor.  Allocates its Krylov workspace
+ * (2 * restart + 2 vectors) on first use.                                 */
+int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const void *b,
+                     void *x, int32_t transpose, double tol, int32_t max_iter,
+                     int32_t restart, void *stream);
 int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st);
 void fdfd_factor_destroy(fdfd_factor *fac);
 

@@ -136,3 +136,19 @@ def test_not_converged_is_reported(eng):
     b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
     with pytest.raises(N.NotConverged):
         fac.solve(b, tol=1e-15, max_iter=0, raise_on_fail=True)
+
+
+@pytest.mark.parametrize("prec", ["c64", "c64tc", "c128"])
+def test_gmres_refinement_matches_superlu(eng, prec):
+    Nx, Ny = 230, 170
+    eps, A, rng = _problem(Nx, Ny, "Hz", seed=12, npml=(12, 12))
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [12, 12], "Hz", 1e-6)
+    fac = eng.Factor(eng.symbolic_for(Nx, Ny), prec, max_nrhs=2).numeric(op)
+    b = rng.standard_normal((2, Nx * Ny)) + 1j * rng.standard_normal((2, Nx * Ny))
+    x = fac.solve(b, tol=1e-11, max_iter=40, method="gmres", raise_on_fail=True).cpu().numpy()
+    assert fac.stats()["rel_residual"] <= 1e-11
+    for k in range(2):
+        assert np.linalg.norm(A @ x[k] - b[k]) / np.linalg.norm(b[k]) < 1e-11
+        assert rel(x[k], O.solve(A, b[k])) < 1e-8
+    xt = fac.solve(b[0], transpose=True, tol=1e-11, max_iter=40, method="gmres", raise_on_fail=True).cpu().numpy()
+    assert np.linalg.norm(A.T @ xt - b[0]) / np.linalg.norm(b[0]) < 1e-11
