@@ -127,7 +127,8 @@ def run_ours(args, rank, world):
 
     def one(fac, prec):
         fac.numeric(op)
-        return fac.solve(b, tol=1e-10, max_iter=5 if prec == "c128" else 40, raise_on_fail=True)
+        return fac.solve(b, tol=1e-10, max_iter=5 if prec == "c128" else 40, raise_on_fail=True,
+                         method="ir" if prec == "c128" else args.method)
 
     def timed(prec, steps, warmup):
         fac = engine.Factor(sym, prec)
@@ -320,7 +321,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=512)
     ap.add_argument("--workload", default="solve", choices=["solve", "serving", "adjoint", "kerr"])
-    ap.add_argument("--precision", default="c64")
+    ap.add_argument("--precision", default="c64tc", choices=["c64tc", "c64", "c128"])
+    ap.add_argument("--method", default="ir", choices=["ir", "gmres"])
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--slots", type=int, default=4)

@@ -154,47 +154,97 @@ __global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__res
 // LU of one nb x nb diagonal block per front (no pivoting), then the two
 // triangular inverses, written back in place.
 template <typename T, typename R>
-__global__ void k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, R tiny,
-                          int *tiny_count) {
+__global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
+                                                 R tiny, int *tiny_count) {
     extern __shared__ unsigned char smem_raw[];
     // Padded leading dimension NB + 1: column and row accesses are both free
     // of shared-memory bank conflicts.
     constexpr int LS = NB + 1;
     T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major, ld LS
     T *X = D + NB * LS;
+    __shared__ T s_col[2][NB], s_row[2][NB];
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
     T *F = pool + f.f_off + (int64_t)k0 * f.ld + k0;
     const int64_t ld = f.ld;
     const int tid = threadIdx.x;
-    for (int idx = tid; idx < w * w; idx += blockDim.x) {
-        const int r = idx % w, c = idx / w;
-        D[r + c * LS] = F[r + c * ld];
-    }
-    __syncthreads();
+    // Register-blocked LU: thread (tx, ty) owns rows tx + 16 i and columns
+    // ty + 16 j (i, j < 4) of the block; step jj broadcasts column jj and
+    // row jj through double-buffered shared memory (one barrier per step).
+    const int tx = tid & 15, ty = tid >> 4;
+    T a[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = tx + 16 * i, c = ty + 16 * j;
+            a[i][j] = (r < w && c < w) ? F[r + (int64_t)c * ld] : czero<T>();
+        }
     for (int jj = 0; jj < w; ++jj) {
-        if (tid == 0) {
-            T pv = D[jj + jj * LS];
-            const R a = sqrt(cabs2(pv));
-            if (!(a >= tiny)) {
-                // Static pivot: keep the phase, lift the modulus to tiny.
-                pv = (a > R(0)) ? cmake<R>(pv.x / a * tiny, pv.y / a * tiny) : cmake<R>(tiny, R(0));
-                D[jj + jj * LS] = pv;
-                atomicAdd(tiny_count, 1);
+        const int buf = jj & 1, jq = jj >> 4, jr = jj & 15;
+        if (ty == jr) {  // owners of column jj (the diagonal owner lifts a tiny pivot)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = tx + 16 * i;
+                T v = czero<T>();
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (j == jq) v = a[i][j];
+                if (r == jj) {
+                    const R am = sqrt(cabs2(v));
+                    if (!(am >= tiny)) {
+                        v = (am > R(0)) ? cmake<R>(v.x / am * tiny, v.y / am * tiny) : cmake<R>(tiny, R(0));
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (j == jq) a[i][j] = v;
+                        atomicAdd(tiny_count, 1);
+                    }
+                }
+                if (r >= jj) s_col[buf][r] = v;
+            }
+        }
+        if (tx == jr) {  // owners of row jj
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = ty + 16 * j;
+                T v = czero<T>();
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (i == jq) v = a[i][j];
+                if (c > jj) s_row[buf][c] = v;
             }
         }
         __syncthreads();
-        const T inv = crecip(D[jj + jj * LS]);
-        for (int r = jj + 1 + tid; r < w; r += blockDim.x) D[r + jj * LS] = cmul(D[r + jj * LS], inv);
-        __syncthreads();
-        const int rem = w - jj - 1;
-        for (int idx = tid; idx < rem * rem; idx += blockDim.x) {
-            const int r = jj + 1 + idx % rem, c = jj + 1 + idx / rem;
-            cmsub(D[r + c * LS], D[r + jj * LS], D[jj + c * LS]);
+        const T inv = crecip(s_col[buf][jj]);
+        T l[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int r = tx + 16 * i;
+            l[i] = (r > jj && r < w) ? cmul(s_col[buf][r], inv) : czero<T>();
         }
-        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = ty + 16 * j;
+            if (c > jj && c < w) {
+                const T u = s_row[buf][c];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) cmsub(a[i][j], l[i], u);
+            } else if (c == jj) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (tx + 16 * i > jj) a[i][j] = l[i];
+            }
+        }
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = tx + 16 * i, c = ty + 16 * j;
+            if (r < w && c < w) D[r + c * LS] = a[i][j];
+        }
+    __syncthreads();
     // inv(L) (unit lower) and inv(U), warp-parallel: a warp owns whole
     // columns of inv(L) / rows of inv(U), two entries per lane in registers,
     // and advances one step per shuffle (axpy form of the substitution).

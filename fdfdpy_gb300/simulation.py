@@ -40,6 +40,9 @@ class Simulation:
         self.xrange = [0, float(Nx * self.dl)]
         self.yrange = [0, float(Ny * self.dl)]
         self.precision = DEFAULT_PRECISION
+        # refinement of mixed-precision solves: 'gmres' (factor-preconditioned
+        # GMRES) or 'ir' (plain iterative refinement); complex128 uses 'ir'
+        self.refinement = 'ir'
         self.last_solve_stats = None
 
         self.eps_r = eps_r
@@ -142,7 +145,8 @@ class Simulation:
         precision = precision or self.precision
         op, key = self._operator(include_nl)
         fac = self._factor_for(op, key, precision)
-        x = fac.solve(b, transpose=transpose, op=op,
+        method = 'ir' if precision == 'c128' else self.refinement
+        x = fac.solve(b, transpose=transpose, op=op, method=method,
                       tol=DEFAULT_TOL[precision] if tol is None else tol,
                       max_iter=DEFAULT_MAX_REFINE[precision] if max_iter is None else max_iter)
         self.last_solve_stats = fac.stats()
