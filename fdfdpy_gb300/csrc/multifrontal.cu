@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, 
     constexpr int LS = NB + 1;
     T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major, ld LS
     T *X = D + NB * LS;
-    __shared__ T s_col[2][NB], s_row[2][NB];
+    __shared__ T s_col[2][NB], s_row[2][NB], s_pinv[2];
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, 
                             if (j == jq) a[i][j] = v;
                         atomicAdd(tiny_count, 1);
                     }
+                    s_pinv[buf] = crecip(v);
                 }
                 if (r >= jj) s_col[buf][r] = v;
             }
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, 
             }
         }
         __syncthreads();
-        const T inv = crecip(s_col[buf][jj]);
+        const T inv = s_pinv[buf];
         T l[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -244,6 +245,10 @@ __global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, 
             const int r = tx + 16 * i, c = ty + 16 * j;
             if (r < w && c < w) D[r + c * LS] = a[i][j];
         }
+    __syncthreads();
+    // reciprocals of U's diagonal, once (the row jobs below are sequential)
+    __shared__ T s_dinv[NB];
+    if (tid < w) s_dinv[tid] = crecip(D[tid + tid * LS]);
     __syncthreads();
     // inv(L) (unit lower) and inv(U), warp-parallel: a warp owns whole
     // columns of inv(L) / rows of inv(U), two entries per lane in registers,
@@ -277,7 +282,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, 
                 if (mine0 || mine1) {
                     const T ac = mine0 ? a0 : a1;
                     const T num = cmake<R>((c == r ? R(1) : R(0)) - ac.x, -ac.y);
-                    yc = cmul(num, crecip(D[c + c * LS]));
+                    yc = cmul(num, s_dinv[c]);
                     if (mine0) y0 = yc; else y1 = yc;
                 }
                 yc.x = __shfl_sync(0xffffffffu, yc.x, c & 31);
