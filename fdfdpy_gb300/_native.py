@@ -90,6 +90,7 @@ SIGNATURES = {
     "fdfd_solve_gmres": (C.c_int, [P, POP, P, P, I32, D, I32, I32, P]),
     "fdfd_factor_stats_get": (C.c_int, [P, C.POINTER(FactorStats)]),
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
+    "fdfd_factor_set_fused_limit": (C.c_int, [P, I32]),
     "fdfd_factor_destroy": (None, [P]),
     "fdfd_profile_enable": (C.c_int, [I32]),
     "fdfd_profile_reset": (C.c_int, []),

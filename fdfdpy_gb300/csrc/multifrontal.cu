@@ -151,154 +151,316 @@ __global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__res
     }
 }
 
-// LU of one nb x nb diagonal block per front (no pivoting), then the two
-// triangular inverses, written back in place.
+// ---- dense LU of one square block in shared memory ------------------------
+// k_dense_lu factors one block per front, held in shared memory (padded to a
+// multiple of 16 with an identity border):
+//   whole = 0: the w x w diagonal block at (k0, k0), all w pivots (the panel
+//              step of a large front; w = min(64, p - k0)),
+//   whole = 1: the complete m x m front with its p <= 64 pivots: L21, U12
+//              and the update matrix come out of the same launch (small
+//              fronts, where four launches per level would each re-read the
+//              front).
+// Right-looking, blocked by 16 columns.  Per block step: one warp factors
+// the 16 x 16 diagonal block in registers (row i in lane i, pivot row
+// broadcast by shuffles) and inverts both triangles (lane q < 16: column q
+// of inv(L); lane 16 + r: row r of inv(U)), writing the inverses in place;
+// then every thread computes rows of L21 = A21 inv(U11) and columns of
+// U12 = inv(L11) A12 as independent dot products, and the trailing block
+// takes a rank-16 update with 4 x 4 register tiles.  At the end the
+// off-diagonal blocks of inv(L) and inv(U) over the pivot block are formed
+// block row by block row with uniform 16 x 16 block products.
+constexpr int kSub = 16;                      // block width
+constexpr int kDenseMaxPiv = NB;              // pivots per launch
+constexpr int kDenseThreads = 256;
+constexpr size_t kDenseSmemMax = 220 * 1024;  // dynamic shared memory of one block
+constexpr int kDiagLd = kSub + 1;
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t dense_lu_smem(int n) {
+    const int S = (n + kSub - 1) / kSub * kSub;
+    return (size_t)S * (S + 1) * sizeof(T);
+}
+
+// 1/b = conj(b) / |b|^2 with a round-to-nearest reciprocal; the operands are
+// pivots of the operator scaled to max|diag| = 1 and at least the static
+// pivot threshold, so |b|^2 stays inside the normal range.
+__device__ __forceinline__ c64 crecip_fast(c64 b) {
+    const float s = __frcp_rn(fmaf(b.x, b.x, b.y * b.y));
+    return cmake<float>(b.x * s, -b.y * s);
+}
+__device__ __forceinline__ c128 crecip_fast(c128 b) {
+    const double s = __drcp_rn(fma(b.x, b.x, b.y * b.y));
+    return cmake<double>(b.x * s, -b.y * s);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_c(T v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One warp: LU of the kw x kw diagonal block at (c0, c0) of D (no
+// pivoting; a pivot below `tiny` in modulus is lifted and counted), then
+// inv(L11) strictly below and inv(U11) on and above the diagonal, in place.
 template <typename T, typename R>
-__global__ void __launch_bounds__(256) k_lu_diag(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
-                                                 R tiny, int *tiny_count) {
-    extern __shared__ unsigned char smem_raw[];
-    // Padded leading dimension NB + 1: column and row accesses are both free
-    // of shared-memory bank conflicts.
-    constexpr int LS = NB + 1;
-    T *D = reinterpret_cast<T *>(smem_raw);  // NB x NB, column-major, ld LS
-    T *X = D + NB * LS;
-    __shared__ T s_col[2][NB], s_row[2][NB], s_pinv[2];
-    const FrontD f = fr[f_begin + blockIdx.x];
-    const int w = min(NB, f.p - k0);
-    if (w <= 0) return;
-    T *F = pool + f.f_off + (int64_t)k0 * f.ld + k0;
-    const int64_t ld = f.ld;
-    const int tid = threadIdx.x;
-    // Register-blocked LU: thread (tx, ty) owns rows tx + 16 i and columns
-    // ty + 16 j (i, j < 4) of the block; step jj broadcasts column jj and
-    // row jj through double-buffered shared memory (one barrier per step).
-    const int tx = tid & 15, ty = tid >> 4;
-    T a[4][4];
+__device__ __forceinline__ void warp_diag_block(T *D, int LD, int c0, int kw, R tiny, int *tiny_count, T *Ls,
+                                               T *dinv) {
+    const int lane = threadIdx.x & 31;
+    const bool row_lane = lane < kw;
+    T a[kSub];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int c = 0; c < kSub; ++c)
+        a[c] = (row_lane && c < kw) ? D[(c0 + lane) + (c0 + c) * LD] : czero<T>();
+    const R tiny2 = tiny * tiny;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int r = tx + 16 * i, c = ty + 16 * j;
-            a[i][j] = (r < w && c < w) ? F[r + (int64_t)c * ld] : czero<T>();
-        }
-    for (int jj = 0; jj < w; ++jj) {
-        const int buf = jj & 1, jq = jj >> 4, jr = jj & 15;
-        if (ty == jr) {  // owners of column jj (the diagonal owner lifts a tiny pivot)
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int r = tx + 16 * i;
-                T v = czero<T>();
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (j == jq) v = a[i][j];
-                if (r == jj) {
-                    const R am = sqrt(cabs2(v));
-                    if (!(am >= tiny)) {
-                        v = (am > R(0)) ? cmake<R>(v.x / am * tiny, v.y / am * tiny) : cmake<R>(tiny, R(0));
-#pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            if (j == jq) a[i][j] = v;
-                        atomicAdd(tiny_count, 1);
-                    }
-                    s_pinv[buf] = crecip(v);
+    for (int t = 0; t < kSub; ++t) {
+        if (t < kw) {
+            T piv = shfl_c(a[t], t);
+            const R m2 = cabs2(piv);
+            if (!(m2 >= tiny2)) {  // lift (all lanes compute the same value)
+                const R am = sqrt(m2);
+                piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
+                if (lane == t) {
+                    a[t] = piv;
+                    atomicAdd(tiny_count, 1);
                 }
-                if (r >= jj) s_col[buf][r] = v;
+            }
+            const T pinv = crecip_fast(piv);
+            if (lane == 0) dinv[t] = pinv;
+            const bool upd = row_lane && lane > t;
+            T l = cmul(a[t], pinv);
+            if (upd) a[t] = l;
+#pragma unroll
+            for (int c = t + 1; c < kSub; ++c) {
+                const T u = shfl_c(a[c], t);
+                if (upd) cmsub(a[c], l, u);
             }
         }
-        if (tx == jr) {  // owners of row jj
+    }
+    if (row_lane)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int c = ty + 16 * j;
-                T v = czero<T>();
+        for (int c = 0; c < kSub; ++c)
+            if (c < kw) Ls[lane + c * kDiagLd] = a[c];
+    __syncwarp();
+    // lane q < 16: column q of inv(L) (x = e_q; x[i] -= L[i][t] x[t]);
+    // lane 16 + r: row r of inv(U) as column r of inv(U^T)
+    // (z = e_r; z[t] *= 1/U[t][t]; z[i] -= U[t][i] z[t]).
+    const bool upper = lane >= kSub;
+    const int q = lane & (kSub - 1);
+    const int si = upper ? kDiagLd : 1, st = upper ? 1 : kDiagLd;
+    T x[kSub];
+#pragma unroll
+    for (int i = 0; i < kSub; ++i) x[i] = (i == q) ? cone<T>() : czero<T>();
+#pragma unroll
+    for (int t = 0; t < kSub; ++t) {
+        if (t < kw && t >= q) {
+            if (upper) x[t] = cmul(x[t], dinv[t]);
+#pragma unroll
+            for (int i = t + 1; i < kSub; ++i)
+                if (i < kw) cmsub(x[i], Ls[i * si + t * st], x[t]);
+        }
+    }
+    if (q < kw) {
+        if (upper) {
+#pragma unroll
+            for (int c = 0; c < kSub; ++c)
+                if (c >= q && c < kw) D[(c0 + q) + (c0 + c) * LD] = x[c];
+        } else {
+#pragma unroll
+            for (int i = 0; i < kSub; ++i)
+                if (i > q && i < kw) D[(c0 + i) + (c0 + q) * LD] = x[i];
+        }
+    }
+}
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 2 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
+                                                            int k0, int whole, R tiny, int *tiny_count) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *D = reinterpret_cast<T *>(smem_raw);
+    __shared__ T s_ls[kSub * kDiagLd];
+    __shared__ T s_dinv[kSub];
+    const FrontD f = fr[f_begin + blockIdx.x];
+    int n, P;
+    T *G;
+    if (whole) {
+        n = f.m;
+        P = f.p;
+        G = pool + f.f_off;
+    } else {
+        P = min(NB, f.p - k0);
+        n = P;
+        G = pool + f.f_off + (int64_t)k0 * f.ld + k0;
+    }
+    if (P <= 0 || n <= 0) return;
+    const int64_t ld = f.ld;
+    const int S = (n + kSub - 1) / kSub * kSub, LD = S + 1, NBLK = S / kSub;
+    if (!whole) P = S;  // the identity border is factored along (no effect)
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int c = warp; c < S; c += kDenseThreads / 32)
+        for (int r = lane; r < S; r += 32) {
+            if (r < n && c < n)
+                cp_async_elem(D + r + c * LD, G + r + (int64_t)c * ld);
+            else
+                D[r + c * LD] = (r == c) ? cone<T>() : czero<T>();
+        }
+    cp_async_wait_all();
+    __syncthreads();
+
+    const int tx = tid & 15, ty = tid >> 4;
+    for (int c0 = 0; c0 < P; c0 += kSub) {
+        const int kw = min(kSub, P - c0), b1 = c0 + kw;
+        if (warp == 0) warp_diag_block<T, R>(D, LD, c0, kw, tiny, tiny_count, s_ls, s_dinv);
+        __syncthreads();
+        // L21 rows [b1, S): a[0:kw] <- a inv(U11);  U12 columns [b1, S): a <- inv(L11) a
+        const int nr = S - b1;
+        for (int item = tid; item < 2 * nr; item += kDenseThreads) {
+            const bool is_row = item < nr;
+            const int idx = b1 + (is_row ? item : item - nr);
+            // element j of the row / column: D[base + j * step]
+            T *base = is_row ? D + idx + c0 * LD : D + c0 + idx * LD;
+            const int step = is_row ? LD : 1;
+            T v[kSub], o[kSub];
+#pragma unroll
+            for (int j = 0; j < kSub; ++j) v[j] = (j < kw) ? base[j * step] : czero<T>();
+            if (is_row) {
+#pragma unroll
+                for (int c = 0; c < kSub; ++c) {
+                    T s = czero<T>();
+#pragma unroll
+                    for (int k = 0; k <= c; ++k)
+                        if (c < kw) cmac(s, v[k], D[(c0 + k) + (c0 + c) * LD]);
+                    o[c] = s;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < kSub; ++i) {
+                    T s = v[i];
+#pragma unroll
+                    for (int k = 0; k < i; ++k)
+                        if (i < kw) cmac(s, D[(c0 + i) + (c0 + k) * LD], v[k]);
+                    o[i] = s;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kSub; ++j)
+                if (j < kw) base[j * step] = o[j];
+        }
+        __syncthreads();
+        // trailing rows/columns [b1, S) -= L21 U12 (rank kw)
+        const int Ilo = b1 / kSub;
+        for (int I0 = Ilo; I0 < NBLK; I0 += 4)
+            for (int J0 = Ilo; J0 < NBLK; J0 += 4) {
+                T acc[4][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
-                    if (i == jq) v = a[i][j];
-                if (c > jj) s_row[buf][c] = v;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (I0 + i < NBLK && J0 + j < NBLK)
+                            acc[i][j] = D[(kSub * (I0 + i) + tx) + (kSub * (J0 + j) + ty) * LD];
+#pragma unroll 4
+                for (int t = 0; t < kw; ++t) {
+                    T l[4], u[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (I0 + i < NBLK) l[i] = D[(kSub * (I0 + i) + tx) + (c0 + t) * LD];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (J0 + j < NBLK) u[j] = D[(c0 + t) + (kSub * (J0 + j) + ty) * LD];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (I0 + i < NBLK && J0 + j < NBLK) cmsub(acc[i][j], l[i], u[j]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (I0 + i < NBLK && J0 + j < NBLK && kSub * (I0 + i) + tx >= b1 &&
+                            kSub * (J0 + j) + ty >= b1)
+                            D[(kSub * (I0 + i) + tx) + (kSub * (J0 + j) + ty) * LD] = acc[i][j];
+            }
+        __syncthreads();
+    }
+
+    // off-diagonal blocks of the inverses over the P x P pivot block, block
+    // row / column B from the ones before it (unit diagonal of inv(L) implied):
+    //   X[B, J] = -inv(L_BB) T,  T = sum_{K=J}^{B-1} L[B, K] X[K, J]
+    //   Y[J, B] = -T' inv(U_BB), T' = sum_{K=J}^{B-1} Y[J, K] U[K, B]
+    const int nbk = (P + kSub - 1) / kSub;
+    constexpr int kMaxB = kDenseMaxPiv / kSub - 1;  // 3
+    for (int B = 1; B < nbk; ++B) {
+        const int b0 = B * kSub, bs = min(kSub, P - b0);
+        T vl[kMaxB], vu[kMaxB];
+#pragma unroll
+        for (int J = 0; J < kMaxB; ++J) {
+            if (J < B) {
+                const int j0 = J * kSub;
+                T sl = czero<T>(), su = czero<T>();
+                // K = J: X[J, J] unit lower (stored strictly below), Y[J, J] upper
+#pragma unroll
+                for (int k = 0; k < kSub; ++k) {
+                    const T xkj = (k == ty) ? cone<T>() : (k > ty ? D[(j0 + k) + (j0 + ty) * LD] : czero<T>());
+                    cmac(sl, D[(b0 + tx) + (j0 + k) * LD], xkj);
+                    if (k >= tx) cmac(su, D[(j0 + tx) + (j0 + k) * LD], D[(j0 + k) + (b0 + ty) * LD]);
+                }
+                for (int K = J + 1; K < B; ++K) {
+                    const int kk = K * kSub;
+#pragma unroll
+                    for (int k = 0; k < kSub; ++k) {
+                        cmac(sl, D[(b0 + tx) + (kk + k) * LD], D[(kk + k) + (j0 + ty) * LD]);
+                        cmac(su, D[(j0 + tx) + (kk + k) * LD], D[(kk + k) + (b0 + ty) * LD]);
+                    }
+                }
+                vl[J] = sl;
+                vu[J] = su;
             }
         }
         __syncthreads();
-        const T inv = s_pinv[buf];
-        T l[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int r = tx + 16 * i;
-            l[i] = (r > jj && r < w) ? cmul(s_col[buf][r], inv) : czero<T>();
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int c = ty + 16 * j;
-            if (c > jj && c < w) {
-                const T u = s_row[buf][c];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) cmsub(a[i][j], l[i], u);
-            } else if (c == jj) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (tx + 16 * i > jj) a[i][j] = l[i];
+        for (int J = 0; J < kMaxB; ++J)
+            if (J < B) {
+                if (tx < bs) D[(b0 + tx) + (J * kSub + ty) * LD] = vl[J];
+                if (ty < bs) D[(J * kSub + tx) + (b0 + ty) * LD] = vu[J];
             }
-        }
-    }
+        __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+        for (int J = 0; J < kMaxB; ++J) {
+            if (J < B) {
+                const int j0 = J * kSub;
+                T sl = D[(b0 + tx) + (j0 + ty) * LD], su = czero<T>();
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int r = tx + 16 * i, c = ty + 16 * j;
-            if (r < w && c < w) D[r + c * LS] = a[i][j];
-        }
-    __syncthreads();
-    // reciprocals of U's diagonal, once (the row jobs below are sequential)
-    __shared__ T s_dinv[NB];
-    if (tid < w) s_dinv[tid] = crecip(D[tid + tid * LS]);
-    __syncthreads();
-    // inv(L) (unit lower) and inv(U), warp-parallel: a warp owns whole
-    // columns of inv(L) / rows of inv(U), two entries per lane in registers,
-    // and advances one step per shuffle (axpy form of the substitution).
-    const int warp = tid >> 5, lane = tid & 31, nwarps = blockDim.x >> 5;
-    for (int job = warp; job < 2 * w; job += nwarps) {
-        if (job < w) {
-            // column c of inv(L): x = e_c; for t >= c: x[t+1:] -= L[t+1:, t] x[t]
-            const int c = job;
-            T x0 = (lane == c) ? cone<T>() : czero<T>();
-            T x1 = (lane + 32 == c) ? cone<T>() : czero<T>();
-            for (int t = c; t < w - 1; ++t) {
-                const T own = (t < 32) ? x0 : x1;
-                T xt;
-                xt.x = __shfl_sync(0xffffffffu, own.x, t & 31);
-                xt.y = __shfl_sync(0xffffffffu, own.y, t & 31);
-                if (lane > t && lane < w) cmsub(x0, D[lane + t * LS], xt);
-                if (lane + 32 > t && lane + 32 < w) cmsub(x1, D[lane + 32 + t * LS], xt);
-            }
-            if (lane > c && lane < w) X[lane + c * LS] = x0;
-            if (lane + 32 > c && lane + 32 < w) X[lane + 32 + c * LS] = x1;
-        } else {
-            // row r of inv(U): y U = e_r; for c >= r: y[c] = (e_r[c] - a[c]) / U[c,c],
-            // then a[c+1:] += y[c] U[c, c+1:]
-            const int r = job - w;
-            T a0 = czero<T>(), a1 = czero<T>();
-            T y0 = czero<T>(), y1 = czero<T>();
-            for (int c = r; c < w; ++c) {
-                const bool mine0 = (lane == c), mine1 = (lane + 32 == c);
-                T yc = czero<T>();
-                if (mine0 || mine1) {
-                    const T ac = mine0 ? a0 : a1;
-                    const T num = cmake<R>((c == r ? R(1) : R(0)) - ac.x, -ac.y);
-                    yc = cmul(num, s_dinv[c]);
-                    if (mine0) y0 = yc; else y1 = yc;
+                for (int k = 0; k < kSub; ++k) {
+                    if (k < tx) cmac(sl, D[(b0 + tx) + (b0 + k) * LD], D[(b0 + k) + (j0 + ty) * LD]);
+                    if (k <= ty && k < bs) cmac(su, D[(j0 + tx) + (b0 + k) * LD], D[(b0 + k) + (b0 + ty) * LD]);
                 }
-                yc.x = __shfl_sync(0xffffffffu, yc.x, c & 31);
-                yc.y = __shfl_sync(0xffffffffu, yc.y, c & 31);
-                if (lane > c && lane < w) cmac(a0, yc, D[c + lane * LS]);
-                if (lane + 32 > c && lane + 32 < w) cmac(a1, yc, D[c + (lane + 32) * LS]);
+                vl[J] = cmake<R>(-sl.x, -sl.y);
+                vu[J] = cmake<R>(-su.x, -su.y);
             }
-            if (lane >= r && lane < w) X[r + lane * LS] = y0;
-            if (lane + 32 >= r && lane + 32 < w) X[r + (lane + 32) * LS] = y1;
         }
+        __syncthreads();
+#pragma unroll
+        for (int J = 0; J < kMaxB; ++J)
+            if (J < B) {
+                if (tx < bs) D[(b0 + tx) + (J * kSub + ty) * LD] = vl[J];
+                if (ty < bs) D[(J * kSub + tx) + (b0 + ty) * LD] = vu[J];
+            }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int idx = tid; idx < w * w; idx += blockDim.x) {
-        const int r = idx % w, c = idx / w;
-        F[r + c * ld] = X[r + c * LS];
-    }
+    for (int c = warp; c < n; c += kDenseThreads / 32)
+        for (int r = lane; r < n; r += 32) G[r + (int64_t)c * ld] = D[r + c * LD];
 }
 
 enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
@@ -447,7 +609,6 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
 // triangle), the input vector block and the result block, staged with
 // coalesced loads so that the dependent triangular product runs out of
 // shared memory instead of waiting on a global load per term.
-constexpr int kPanelSmemElems = NB * NB;  // + 2 * nrhs * NB
 template <typename T>
 __host__ __device__ __forceinline__ size_t panel_smem_bytes(int nrhs) {
     return (size_t)(NB * NB + 2 * nrhs * NB) * sizeof(T);
@@ -865,11 +1026,18 @@ struct fdfd_factor {
     int *d_solve_err = nullptr;
     int64_t *d_coop_off = nullptr;
     void *d_coop_scratch = nullptr;
+    // pipelined panel units of the cooperative levels (per level: forward
+    // list, backward list) and their completion flags
+    int2 *d_units = nullptr;
+    std::vector<int> unit_fwd_off, unit_fwd_n, unit_bwd_off, unit_bwd_n, lev_kp;
+    unsigned *d_flags = nullptr;
+    unsigned epoch = 0;
     // two-pass backward opener for levels with wide fronts
     std::vector<char> bwd_wide;
     int64_t *d_bwd_off = nullptr;
     void *d_bwd_scratch = nullptr;
     double pivot_tol = -1.0;  // relative static-pivot threshold (<0: default)
+    int fused_max_m = -1;     // largest front factored in one launch (<0: shared-memory limit)
     // tensor-core Schur path (FDFD_PREC_C64_TC)
     bool use_tc = false;
     std::vector<char> tc_level;
@@ -887,6 +1055,15 @@ struct fdfd_factor {
 namespace fdfd {
 namespace {
 
+
+// A level is factored front-by-front in one launch when all its fronts have
+// at most 64 pivots and the largest front fits in shared memory.
+template <typename T>
+bool dense_front_fits(const fdfd_factor *fac, int maxp, int maxm) {
+    if (maxp > kDenseMaxPiv || maxm <= 0) return false;
+    if (fac->fused_max_m >= 0 && maxm > fac->fused_max_m) return false;
+    return dense_lu_smem<T>(maxm) <= kDenseSmemMax;
+}
 
 template <typename T, typename R>
 int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
@@ -926,10 +1103,18 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             }
         }
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
+        if (dense_front_fits<T>(fac, maxp, maxm)) {
+            // every front of the level in one launch: LU, L21, U12 and the update matrix
+            prof_begin(PROF_LU_DIAG, st);
+            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(maxm), st>>>(fac->d_fronts, pool, fb, 0, 1,
+                                                                                  tiny, fac->d_tiny);
+            prof_end(PROF_LU_DIAG, st, 1);
+            continue;
+        }
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
-            k_lu_diag<T, R><<<nfl, 256, 2 * NB * (NB + 1) * sizeof(T), st>>>(fac->d_fronts, pool, fb, k0,
-                                                                             tiny, fac->d_tiny);
+            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), st>>>(fac->d_fronts, pool, fb, k0, 0,
+                                                                                tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             const int trail = maxm - k0 - 1;  // upper bound of m - t0
             if (trail <= 0) continue;
@@ -994,12 +1179,137 @@ __device__ bool grid_sync(GridBar *gb, int *err) {
     return s_ok != 0;
 }
 
+// Completion flags of the pipelined panel units.  A unit publishes its
+// result, then (thread 0, after a fence) stores the launch's epoch into its
+// flag with release semantics; a consumer's thread 0 polls with acquire
+// semantics and the block reads the result through L2 after a barrier.
+// Epochs differ between launches, so flags never need clearing.  The poll is
+// bounded: after kFlagLimit rounds, or once another CTA has reported a
+// failure, the CTA records the error and the block returns.
+constexpr unsigned kFlagLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ bool wait_flag(const unsigned *flag, unsigned epoch, int *err) {
+    __shared__ int s_go;
+    if (threadIdx.x == 0) {
+        int go = 1;
+        for (unsigned it = 0; ld_acquire_u32(flag) != epoch; ++it) {
+            if (it > kFlagLimit || ((it & 1023u) == 1023u && *(volatile int *)err != 0)) {
+                go = 0;
+                atomicExch(err, 1);
+                break;
+            }
+            __nanosleep(16);
+        }
+        s_go = go;
+    }
+    __syncthreads();
+    return s_go != 0;
+}
+
+__device__ __forceinline__ void publish_flag(unsigned *flag, unsigned epoch) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        st_release_u32(flag, epoch);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T ldcg_c(const T *p);
+template <>
+__device__ __forceinline__ c64 ldcg_c<c64>(const c64 *p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
+    return cmake<float>(v.x, v.y);
+}
+template <>
+__device__ __forceinline__ c128 ldcg_c<c128>(const c128 *p) {
+    const double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
+    return cmake<double>(v.x, v.y);
+}
+
+// Pipelined panel unit, the shared part: acc[rhs] (four partial sums per
+// row, rows rr = tid / 4 of the block) -= F[rows, panel] v_panel for each
+// panel in order, where v_panel (a 64-vector per rhs) is read from vsrc
+// (stride sum_m) once the panel's flag carries the epoch.  The panel's
+// matrix tile is loaded before the wait.
+template <typename T>
+__device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool live, int k_first, int k_last,
+                                            int k_step, int p, const T *vsrc, int64_t sum_m, int nrhs,
+                                            const unsigned *flags, unsigned epoch, int *err, T *vs,
+                                            T (&acc)[8]) {
+    const int rr = threadIdx.x >> 2, t0 = 16 * (threadIdx.x & 3);
+    for (int k = k_first; k != k_last; k += k_step) {
+        const int c0 = k * NB, w = min(NB, p - c0);
+        T a[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+            a[i] = (live && t0 + i < w) ? F[(r0 + rr) + (int64_t)(c0 + t0 + i) * ld] : czero<T>();
+        if (!wait_flag(flags + k, epoch, err)) return false;
+        for (int idx = threadIdx.x; idx < nrhs * NB; idx += blockDim.x) {
+            const int r = idx / NB, i = idx % NB;
+            vs[idx] = (i < w) ? ldcg_c(vsrc + r * sum_m + c0 + i) : czero<T>();
+        }
+        __syncthreads();
+        for (int r = 0; r < nrhs; ++r) {
+            const T *vr = vs + r * NB + t0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) cmac(acc[r], a[i], vr[i]);
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// Stage the triangle of the diagonal block's inverse (UPPER: on and above
+// the diagonal; else strictly below) into Ds (ld NB).
+template <typename T, bool UPPER>
+__device__ __forceinline__ void stage_diag(const T *F, int64_t ld, int r0, int rn, T *Ds) {
+    for (int c = threadIdx.x >> 6; c < rn; c += blockDim.x >> 6) {
+        const int r = threadIdx.x & 63;
+        if (r < rn) {
+            const bool need = UPPER ? (r <= c) : (r > c);
+            Ds[r + c * NB] = need ? F[(r0 + r) + (int64_t)(r0 + c) * ld] : czero<T>();
+        }
+    }
+}
+
+// out[rhs][row] = sum_t Ds[row, t] vin[rhs][t] (+ vin[row] for the unit lower
+// inverse), four threads per row; returns the value for q == 0 threads.
+template <typename T, bool UPPER>
+__device__ __forceinline__ T diag_rows(const T *Ds, const T *vr, int rn, int row) {
+    const int q = threadIdx.x & 3;
+    T s = czero<T>();
+    if (row < rn) {
+        if (UPPER) {
+            for (int t = row + q; t < rn; t += 4) cmac(s, Ds[row + t * NB], vr[t]);
+        } else {
+            for (int t = q; t < row; t += 4) cmac(s, Ds[row + t * NB], vr[t]);
+        }
+    }
+    for (int off = 1; off < 4; off <<= 1) {
+        s.x += __shfl_xor_sync(0xffffffffu, s.x, off);
+        s.y += __shfl_xor_sync(0xffffffffu, s.y, off);
+    }
+    if (!UPPER && row < rn) s = cadd(s, vr[row]);
+    return s;
+}
+
 template <typename T, typename R>
 __global__ void __launch_bounds__(kRowsPerCta)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
-                int *err) {
+                int *err, const int2 *__restrict__ units, int nunits, int kpm, unsigned *flags,
+                unsigned epoch) {
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
     // gather: right-hand side of the pivots and the children's updates
@@ -1027,27 +1337,49 @@ __global__ void __launch_bounds__(kRowsPerCta)
         }
     }
     if (!grid_sync(gb, err)) return;
-    for (int k0 = 0; k0 < maxp; k0 += NB) {
-        const int maxch = max(1, (maxm - k0 + kItemRows - 1) / kItemRows);
-        for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
-            const int fi = item / maxch, c = item % maxch;
-            const FrontD f = fr[fb + fi];
-            const int w = min(NB, f.p - k0);
-            if (w <= 0) continue;
-            const int t0 = k0 + w, rbase = t0 + c * kItemRows;
-            if (c > 0 && rbase >= f.m) continue;
-            const T *F = pool + f.f_off;
-            T *yk = panel_diag_apply<T, R, false>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
-                                                  reinterpret_cast<T *>(smem_raw));
-            if (c == 0)
-                for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-                    const int r = idx / w, row = idx % w;
-                    Y[r * sum_m + f.voff + k0 + row] = yk[r * NB + row];
-                }
-            panel_rows_update(F, f.ld, k0, w, rbase, f.m, yk, nrhs, W + f.voff, sum_m);
+    (void)maxp;
+    (void)maxm;
+    // pipelined panels: unit (front, row block R); a pivot block computes
+    // y_R = inv(L_RR) (w_R - sum_k L[R, k] y_k) and publishes it, an update
+    // block accumulates w_B -= sum_k L[B, k] y_k for the parent's gather
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    T *Ds = sm, *vin = sm + NB * NB;
+    const int rr = tid >> 2, q = tid & 3;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int2 un = units[u];
+        const int fi = un.x, rb = un.y;
+        const FrontD f = fr[fb + fi];
+        const int KP = (f.p + NB - 1) / NB;
+        const bool piv = rb < KP;
+        const int r0 = piv ? rb * NB : f.p + (rb - KP) * NB;
+        const int rn = min(NB, (piv ? f.p : f.m) - r0);
+        const T *F = pool + f.f_off;
+        const int64_t ld = f.ld;
+        if (piv) stage_diag<T, false>(F, ld, r0, rn, Ds);
+        const bool live = rr < rn;
+        T acc[8];
+        for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+        if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs,
+                         flags + fi * kpm, epoch, err, vin, acc))
+            return;
+        quad_reduce(acc, nrhs);
+        if (piv) {
+            if (live && q == 0)
+                for (int r = 0; r < nrhs; ++r)
+                    vin[r * NB + rr] = csub(ldcg_c(W + r * sum_m + f.voff + r0 + rr), acc[r]);
             __syncthreads();
+            for (int r = 0; r < nrhs; ++r) {
+                const T y = diag_rows<T, false>(Ds, vin + r * NB, rn, rr);
+                if (live && q == 0) Y[r * sum_m + f.voff + r0 + rr] = y;
+            }
+            publish_flag(flags + fi * kpm + rb, epoch);
+        } else if (live && q == 0) {
+            for (int r = 0; r < nrhs; ++r) {
+                T *d = W + r * sum_m + f.voff + r0 + rr;
+                *d = csub(ldcg_c(d), acc[r]);
+            }
         }
-        if (!grid_sync(gb, err)) return;
+        __syncthreads();
     }
 }
 
@@ -1055,7 +1387,8 @@ template <typename T, typename R>
 __global__ void __launch_bounds__(kRowsPerCta)
     k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
-                T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err) {
+                T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
+                const int2 *__restrict__ units, int nunits, int kpm, unsigned *flags, unsigned epoch) {
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
@@ -1104,36 +1437,47 @@ __global__ void __launch_bounds__(kRowsPerCta)
         }
     }
     if (!grid_sync(gb, err)) return;
-    for (int k0 = ((maxp - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
-        const int maxch = max(1, (k0 + kItemRows - 1) / kItemRows);
-        for (int item = blockIdx.x; item < nfl * maxch; item += gridDim.x) {
-            const int fi = item / maxch, c = item % maxch;
-            const FrontD f = fr[fb + fi];
-            const int w = min(NB, f.p - k0);
-            if (w <= 0) continue;
-            const int rbase = c * kItemRows;
-            if (c > 0 && rbase >= k0) continue;
-            const T *F = pool + f.f_off;
-            T *xk = panel_diag_apply<T, R, true>(F, f.ld, k0, w, W + f.voff, sum_m, nrhs,
-                                                 reinterpret_cast<T *>(smem_raw));
-            if (c == 0) {
-                const int32_t *v = vars + f.voff + k0;
-                for (int idx = tid; idx < nrhs * w; idx += blockDim.x) {
-                    const int r = idx / w, row = idx % w;
-                    x[r * n + v[row]] = to_c128(xk[r * NB + row], 1.0);
-                }
+    // pipelined panels, descending: x_R = inv(U_RR) (acc_R - sum_{j>R} U[R, j] x_j),
+    // published in W's pivot rows (and written to the global solution)
+    T *Ds = xs, *vin = xs + NB * NB;
+    const int rr = tid >> 2, q = tid & 3;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int2 un = units[u];
+        const int fi = un.x, rb = un.y;
+        const FrontD f = fr[fb + fi];
+        const int KP = (f.p + NB - 1) / NB;
+        const int r0 = rb * NB, rn = min(NB, f.p - r0);
+        const T *F = pool + f.f_off;
+        const int64_t ld = f.ld;
+        stage_diag<T, true>(F, ld, r0, rn, Ds);
+        const bool live = rr < rn;
+        T acc[8];
+        for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
+        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, W + f.voff, sum_m, nrhs, flags + fi * kpm,
+                         epoch, err, vin, acc))
+            return;
+        quad_reduce(acc, nrhs);
+        if (live && q == 0)
+            for (int r = 0; r < nrhs; ++r)
+                vin[r * NB + rr] = csub(ldcg_c(W + r * sum_m + f.voff + r0 + rr), acc[r]);
+        __syncthreads();
+        const int32_t *v = vars + f.voff + r0;
+        for (int r = 0; r < nrhs; ++r) {
+            const T xv = diag_rows<T, true>(Ds, vin + r * NB, rn, rr);
+            if (live && q == 0) {
+                W[r * sum_m + f.voff + r0 + rr] = xv;
+                x[r * n + v[rr]] = to_c128(xv, 1.0);
             }
-            panel_rows_update(F, f.ld, k0, w, rbase, k0, xk, nrhs, W + f.voff, sum_m);
-            __syncthreads();
         }
-        if (!grid_sync(gb, err)) return;
+        publish_flag(flags + fi * kpm + rb, epoch);
+        __syncthreads();
     }
 }
 
 template <typename T, typename R>
 int set_smem_attrs() {
-    CUDA_TRY(cudaFuncSetAttribute(k_lu_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(2 * NB * (NB + 1) * sizeof(T))));
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDenseSmemMax));
     const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
@@ -1144,6 +1488,12 @@ int set_smem_attrs() {
 
 // x = A^-1 b for nrhs columns (b, x complex128 on device; may alias d_tmp).
 // s_in / s_out are device arrays of per-column scales.
+// Epoch of the next cooperative launch (never 0, the value flags start at).
+inline unsigned next_epoch(fdfd_factor *fac) {
+    if (++fac->epoch == 0) ++fac->epoch;
+    return fac->epoch;
+}
+
 template <typename T, typename R>
 int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
@@ -1160,12 +1510,17 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             int maxp = S.lev_max_p[L], maxm = S.lev_max_m[L];
             GridBar *gb = (GridBar *)fac->d_bar;
             int *err = fac->d_solve_err;
+            const int2 *units = fac->d_units + fac->unit_fwd_off[L];
+            int nunits = fac->unit_fwd_n[L], kpm = fac->lev_kp[L];
+            unsigned *flags = fac->d_flags;
+            unsigned epoch = next_epoch(fac);
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
-                            (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err};
+                            (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err,
+                            (void *)&units, (void *)&nunits, (void *)&kpm, (void *)&flags, (void *)&epoch};
             // grid: the most work items any phase of this level has, capped
-            // at the co-resident limit (fewer CTAs make cheaper barriers)
-            const int items = std::max(nfl, nfl * ((maxm + kItemRows - 1) / kItemRows));
+            // at the co-resident limit
+            const int items = std::max(nfl, nunits);
             const int grid = std::max(1, std::min(fac->coop_grid, items));
             CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
@@ -1194,13 +1549,18 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             GridBar *gb = (GridBar *)fac->d_bar;
             int *err = fac->d_solve_err;
             T *scr = (T *)fac->d_coop_scratch;
+            const int2 *units = fac->d_units + fac->unit_bwd_off[L];
+            int nunits = fac->unit_bwd_n[L], kpm = fac->lev_kp[L];
+            unsigned *flags = fac->d_flags;
+            unsigned epoch = next_epoch(fac);
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxpp, (void *)&maxb,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
                             (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
-                            (void *)&gb, (void *)&err};
+                            (void *)&gb, (void *)&err, (void *)&units, (void *)&nunits, (void *)&kpm,
+                            (void *)&flags, (void *)&epoch};
             const int prw = (maxpp + kItemRows - 1) / kItemRows;
             const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
-            const int items = std::max(nfl * prw * cch, nfl);
+            const int items = std::max(std::max(nfl * prw * cch, nfl), nunits);
             const int grid = std::max(1, std::min(fac->coop_grid, items));
             CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
@@ -1296,7 +1656,8 @@ void free_factor(fdfd_factor *f) {
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
                     f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
-                    f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch, f->d_krylov};
+                    f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch, f->d_krylov,
+                    f->d_units, f->d_flags};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -1383,6 +1744,53 @@ int64_t coop_layout(const Symbolic &S, int max_nrhs, std::vector<char> *lev, std
     return best;
 }
 
+// Work units of the pipelined substitutions on the cooperative levels, one
+// per (front, block of up to 64 rows).  Forward list: pivot blocks R < KP
+// (rows [64R, min(64R + 64, p))) and update-row blocks numbered KP, KP+1, ...
+// (rows p + 64 (R - KP) ...), sorted by R; backward list: pivot blocks sorted
+// by KP - 1 - R.  A unit waits only on units of its own front that come
+// earlier in its list, so CTAs that take the units in list order (all CTAs
+// co-resident) always make progress.  Returns the number of flags needed
+// (the most fronts x panels of any cooperative level).
+struct PipeLayout {
+    std::vector<int2> units;
+    std::vector<int> fwd_off, fwd_n, bwd_off, bwd_n, kp;
+    int64_t flags = 0;
+};
+PipeLayout pipe_layout(const Symbolic &S) {
+    PipeLayout pl;
+    pl.fwd_off.assign(S.nlev, 0);
+    pl.fwd_n.assign(S.nlev, 0);
+    pl.bwd_off.assign(S.nlev, 0);
+    pl.bwd_n.assign(S.nlev, 0);
+    pl.kp.assign(S.nlev, 0);
+    for (int L = 0; L < S.nlev; ++L) {
+        const int kpm = (S.lev_max_p[L] + NB - 1) / NB;
+        if (kpm < kCoopPanels) continue;
+        const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
+        pl.kp[L] = kpm;
+        pl.flags = std::max<int64_t>(pl.flags, (int64_t)nfl * kpm);
+        int rmax = 0;
+        for (int f = fb; f < fb + nfl; ++f)
+            rmax = std::max(rmax, (S.p[f] + NB - 1) / NB + (S.m[f] - S.p[f] + NB - 1) / NB);
+        pl.fwd_off[L] = (int)pl.units.size();
+        for (int R = 0; R < rmax; ++R)
+            for (int f = fb; f < fb + nfl; ++f) {
+                const int kp = (S.p[f] + NB - 1) / NB, kb = (S.m[f] - S.p[f] + NB - 1) / NB;
+                if (R < kp + kb) pl.units.push_back(make_int2(f - fb, R));
+            }
+        pl.fwd_n[L] = (int)pl.units.size() - pl.fwd_off[L];
+        pl.bwd_off[L] = (int)pl.units.size();
+        for (int d = 0; d < kpm; ++d)
+            for (int f = fb; f < fb + nfl; ++f) {
+                const int kp = (S.p[f] + NB - 1) / NB;
+                if (d < kp) pl.units.push_back(make_int2(f - fb, kp - 1 - d));
+            }
+        pl.bwd_n[L] = (int)pl.units.size() - pl.bwd_off[L];
+    }
+    return pl;
+}
+
 int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     const int64_t elem = precision == FDFD_PREC_C128 ? 16 : 8;
     const int64_t n = (int64_t)S.Nx * S.Ny;
@@ -1396,6 +1804,8 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
     b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
     b += coop_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8 + 16;
+    const PipeLayout pl = pipe_layout(S);
+    b += (int64_t)pl.units.size() * sizeof(int2) + pl.flags * 4;
     return b;
 }
 
@@ -1538,6 +1948,22 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
             if (e == cudaSuccess) e = cudaMemset(f->d_solve_err, 0, 4);
             if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
         }
+        if (rc == FDFD_OK) {
+            PipeLayout pl = pipe_layout(S);
+            f->unit_fwd_off = pl.fwd_off;
+            f->unit_fwd_n = pl.fwd_n;
+            f->unit_bwd_off = pl.bwd_off;
+            f->unit_bwd_n = pl.bwd_n;
+            f->lev_kp = pl.kp;
+            if (!alloc((void **)&f->d_units, pl.units.size() * sizeof(int2)) ||
+                !alloc((void **)&f->d_flags, pl.flags * sizeof(unsigned))) {
+                free_factor(f);
+                return fail(FDFD_ERR_OOM, "factor_create: pipelined-solve allocation failed");
+            }
+            e = cudaMemcpy(f->d_units, pl.units.data(), pl.units.size() * sizeof(int2), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemset(f->d_flags, 0, std::max<int64_t>(pl.flags, 1) * sizeof(unsigned));
+            if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+        }
     }
     if (rc == FDFD_OK) {
         std::vector<int64_t> boff;
@@ -1562,6 +1988,13 @@ extern "C" int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol) {
     if (!(rel_tol >= 0.0) && rel_tol != -1.0)
         return fail(FDFD_ERR_BAD_ARG, "factor_set_pivot_tol: tolerance must be >= 0 (or -1 for the default)");
     fac->pivot_tol = rel_tol;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_set_fused_limit(fdfd_factor *fac, int32_t max_m) {
+    if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_set_fused_limit: NULL factor");
+    if (max_m < -1) return fail(FDFD_ERR_BAD_ARG, "factor_set_fused_limit: max_m must be >= -1");
+    fac->fused_max_m = max_m;
     return FDFD_OK;
 }
 
@@ -1643,7 +2076,7 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
         CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (*fac->h_err)
-            return fail(FDFD_ERR_CUDA, "solve_refined: a grid barrier of the cooperative solve timed out");
+            return fail(FDFD_ERR_CUDA, "solve_refined: a wait of the cooperative solve timed out");
         worst = 0.0;
         for (int r = 0; r < nrhs; ++r) {
             const double rel = bnorm[r] > 0 ? fac->h_norm[r] / bnorm[r] : fac->h_norm[r];
@@ -1795,7 +2228,7 @@ extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const
     }
     CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    if (*fac->h_err) return fail(FDFD_ERR_CUDA, "solve_gmres: a grid barrier of the cooperative solve timed out");
+    if (*fac->h_err) return fail(FDFD_ERR_CUDA, "solve_gmres: a wait of the cooperative solve timed out");
     CUDA_TRY(cudaEventRecord(fac->ev[3], st));
     fac->stats.refine_iters = apps - 1;
     fac->stats.rel_residual = rel;

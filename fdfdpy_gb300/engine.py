@@ -234,7 +234,7 @@ def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
 class Factor:
     """A numeric multifrontal factorization of one operator on the device."""
 
-    def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1, pivot_tol=None):
+    def __init__(self, sym: Symbolic, precision="c128", max_nrhs=1, pivot_tol=None, fused_max_m=None):
         if precision not in N.PREC:
             raise ValueError("precision must be 'c128', 'c64' or 'c64tc'")
         device()
@@ -244,6 +244,8 @@ class Factor:
         self.handle = h
         if pivot_tol is not None:
             N.call("fdfd_factor_set_pivot_tol", h, float(pivot_tol))
+        if fused_max_m is not None:
+            N.call("fdfd_factor_set_fused_limit", h, int(fused_max_m))
         self.op = None
 
     @staticmethod

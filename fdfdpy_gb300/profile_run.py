@@ -1,0 +1,64 @@
+"""One factorization and one factor application of the benchmark workload
+inside NVTX ranges, for profiling the kernels with a launch list:
+
+    ncu --nvtx --nvtx-include "factor_c64tc/" --nvtx-include "solve_c64tc/" \
+        --metrics gpu__time_duration.sum --clock-control none --csv \
+        --log-file launches.csv python -m fdfdpy_gb300.profile_run --size 2048
+
+Each precision first runs once outside the ranges (warm-up: module load,
+first-touch of the factor memory), then once inside `factor_<precision>`
+and `solve_<precision>`.  The workload is the benchmark's: Hz, dl = 0.01,
+NPML = [20, 20], eps in 16 x 16-cell blocks from {1, 12.25}, line source.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+import torch
+
+from . import engine
+from .constants import C_0
+
+
+def workload(N: int):
+    rng = np.random.default_rng(0)
+    eps = np.kron(rng.choice([1.0, 12.25], size=(N // 16, N // 16)), np.ones((16, 16)))
+    src = np.zeros((N, N))
+    src[30, :] = 1.0
+    return eps, src
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--precision", nargs="+", default=["c64", "c64tc"], choices=["c128", "c64", "c64tc"])
+    ap.add_argument("--nrhs", type=int, default=1)
+    args = ap.parse_args(argv)
+    N = args.size
+    eps, src = workload(N)
+    om = 2 * np.pi * C_0 / 1.55e-6
+    op = engine.DeviceOperator(om, eps, N * 0.01, N * 0.01, [20, 20], "Hz", 1e-6)
+    b = engine.as_c128(1j * om * src).reshape(1, -1).repeat(args.nrhs, 1)
+    sym = engine.symbolic_for(N, N)
+    for prec in args.precision:
+        fac = engine.Factor(sym, prec, max_nrhs=args.nrhs)
+        fac.numeric(op)
+        fac.apply_inverse(b)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(f"factor_{prec}")
+        fac.numeric(op)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_push(f"solve_{prec}")
+        fac.apply_inverse(b)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        st = fac.stats()
+        print(f"{prec}: factor {st['factor_ms']:.1f} ms, solve {st['solve_ms']:.2f} ms, "
+              f"tiny pivots {st['tiny_pivots']}")
+        del fac
+
+
+if __name__ == "__main__":
+    main()

@@ -152,3 +152,64 @@ def test_gmres_refinement_matches_superlu(eng, prec):
         assert rel(x[k], O.solve(A, b[k])) < 1e-8
     xt = fac.solve(b[0], transpose=True, tol=1e-11, max_iter=40, method="gmres", raise_on_fail=True).cpu().numpy()
     assert np.linalg.norm(A.T @ xt - b[0]) / np.linalg.norm(b[0]) < 1e-11
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("leaf", [16, 64])
+def test_whole_front_and_panel_kernels_agree(eng, prec, leaf):
+    """Small fronts factored in one launch per level (the whole front in
+    shared memory) and the same fronts through the per-panel kernels give
+    the same solution, and both match SuperLU."""
+    Nx, Ny = 150, 122
+    eps, A, rng = _problem(Nx, Ny, "Hz", seed=21, npml=(10, 10))
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [10, 10], "Hz", 1e-6)
+    sym = eng.Symbolic(Nx, Ny, leaf)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    xr = O.solve(A, b)
+    xs = []
+    for limit in (-1, 0):
+        fac = eng.Factor(sym, prec, fused_max_m=limit).numeric(op)
+        x0 = fac.apply_inverse(b).cpu().numpy()  # one application, no refinement
+        if prec == "c128":
+            assert rel(x0, xr) < 1e-10, limit
+        else:
+            assert rel(x0, xr) < 1e-2, limit
+        x = fac.solve(b, tol=1e-12 if prec == "c128" else 1e-10, max_iter=40, raise_on_fail=True)
+        xs.append(x.cpu().numpy())
+        assert rel(xs[-1], xr) < (1e-10 if prec == "c128" else 1e-8), limit
+    assert rel(xs[0], xs[1]) < (1e-10 if prec == "c128" else 1e-8)
+
+
+def test_static_pivot_lifts_are_counted_on_both_paths(eng):
+    Nx, Ny = 90, 90
+    eps, A, rng = _problem(Nx, Ny, "Ez", seed=22)
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Ez", 1e-6)
+    sym = eng.Symbolic(Nx, Ny, 64)
+    counts = []
+    for limit in (-1, 0):
+        fac = eng.Factor(sym, "c128", pivot_tol=0.3, fused_max_m=limit).numeric(op)
+        counts.append(fac.stats()["tiny_pivots"])
+    assert counts[0] > 0 and counts[1] > 0
+    # same pivots up to rounding: only values at the threshold may differ
+    assert abs(counts[0] - counts[1]) <= max(2, counts[0] // 10)
+
+
+@pytest.mark.parametrize("prec,nrhs", [("c128", 1), ("c128", 3), ("c64", 2)])
+def test_cooperative_levels_solve(eng, prec, nrhs):
+    """A grid large enough that the top levels (separators of >= 256
+    unknowns) run the pipelined cooperative substitutions, forward and
+    transposed, checked by the residual of the operator (scipy CSR)."""
+    Nx, Ny = 700, 520
+    eps, A, rng = _problem(Nx, Ny, "Hz", seed=31, npml=(15, 15))
+    op = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [15, 15], "Hz", 1e-6)
+    fac = eng.Factor(eng.symbolic_for(Nx, Ny), prec, max_nrhs=nrhs).numeric(op)
+    b = rng.standard_normal((nrhs, Nx * Ny)) + 1j * rng.standard_normal((nrhs, Nx * Ny))
+    tol = 1e-9 if prec == "c128" else 1e-2  # one application of the complex64 factor
+    for transpose in (False, True):
+        x = fac.apply_inverse(b, transpose=transpose).cpu().numpy().reshape(nrhs, -1)
+        M = A.T.tocsr() if transpose else A
+        for k in range(nrhs):
+            assert np.linalg.norm(M @ x[k] - b[k]) / np.linalg.norm(b[k]) < tol, (transpose, k)
+    x = fac.solve(b, tol=1e-11, max_iter=30, raise_on_fail=True).cpu().numpy().reshape(nrhs, -1)
+    for k in range(nrhs):
+        assert np.linalg.norm(A @ x[k] - b[k]) / np.linalg.norm(b[k]) < 1e-11
