@@ -160,24 +160,25 @@ __global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__res
 //              and the update matrix come out of the same launch (small
 //              fronts, where four launches per level would each re-read the
 //              front).
-// Right-looking, blocked by 16 columns.  Per block step: one warp factors
-// the 16 x 16 diagonal block in registers (row i in lane i, pivot row
-// broadcast by shuffles) and inverts both triangles (lane q < 16: column q
-// of inv(L); lane 16 + r: row r of inv(U)), writing the inverses in place;
-// then every thread computes rows of L21 = A21 inv(U11) and columns of
-// U12 = inv(L11) A12 as independent dot products, and the trailing block
-// takes a rank-16 update with 4 x 4 register tiles.  At the end the
-// off-diagonal blocks of inv(L) and inv(U) over the pivot block are formed
-// block row by block row with uniform 16 x 16 block products.
-constexpr int kSub = 16;                      // block width
+// Right-looking in steps of 4 pivots: one warp factors and inverts the
+// 4 x 4 diagonal block in registers, one thread per row / column forms
+// L21 = A21 inv(U11) and U12 = inv(L11) A12, and all threads apply the
+// rank-4 update with 4 x 4 register tiles.  The loop bodies are small and
+// the same for every step, so they stay in the instruction cache (a fully
+// unrolled factorization ran several times slower, fetching instructions).
+// Afterwards the pivot block's inverses are completed 4 rows at a time:
+//   X[B, 0:b0] = -inv(L_BB) L[B, 0:b0] X[0:b0, 0:b0]     (unit diagonals)
+//   Y[0:b0, B] = -Y[0:b0, 0:b0] U[0:b0, B] inv(U_BB)
+// with four threads per output column (row) splitting the sum and a quad
+// shuffle to combine them.
+constexpr int kStep = 4;                      // pivots per step
 constexpr int kDenseMaxPiv = NB;              // pivots per launch
 constexpr int kDenseThreads = 256;
 constexpr size_t kDenseSmemMax = 220 * 1024;  // dynamic shared memory of one block
-constexpr int kDiagLd = kSub + 1;
 
 template <typename T>
 __host__ __device__ __forceinline__ size_t dense_lu_smem(int n) {
-    const int S = (n + kSub - 1) / kSub * kSub;
+    const int S = (n + 15) / 16 * 16;
     return (size_t)S * (S + 1) * sizeof(T);
 }
 
@@ -194,13 +195,6 @@ __device__ __forceinline__ c128 crecip_fast(c128 b) {
 }
 
 template <typename T>
-__device__ __forceinline__ T shfl_c(T v, int src) {
-    v.x = __shfl_sync(0xffffffffu, v.x, src);
-    v.y = __shfl_sync(0xffffffffu, v.y, src);
-    return v;
-}
-
-template <typename T>
 __device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
     if (sizeof(T) == 8)
@@ -210,87 +204,87 @@ __device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// One warp: LU of the kw x kw diagonal block at (c0, c0) of D (no
-// pivoting; a pivot below `tiny` in modulus is lifted and counted), then
-// inv(L11) strictly below and inv(U11) on and above the diagonal, in place.
+template <typename T>
+__device__ __forceinline__ T shfl_c(T v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    return v;
+}
+
+// Warp 0: LU (no pivoting; a pivot below `tiny` in modulus is lifted and
+// counted) of the kw x kw block at B (leading dimension LD), then inv(L)
+// strictly below and inv(U) on and above the diagonal, in place.  Lane i < 4
+// holds row i; the pivot row travels by shuffles; lane q then forms column q
+// of inv(L) and row q of inv(U).
 template <typename T, typename R>
-__device__ __forceinline__ void warp_diag_block(T *D, int LD, int c0, int kw, R tiny, int *tiny_count, T *Ls,
-                                               T *dinv) {
+__device__ __forceinline__ void lu4_inv_warp(T *B, int LD, int kw, R tiny, int *tiny_count) {
     const int lane = threadIdx.x & 31;
-    const bool row_lane = lane < kw;
-    T a[kSub];
+    const bool mine = lane < kStep;
+    T a[kStep];
 #pragma unroll
-    for (int c = 0; c < kSub; ++c)
-        a[c] = (row_lane && c < kw) ? D[(c0 + lane) + (c0 + c) * LD] : czero<T>();
+    for (int j = 0; j < kStep; ++j)
+        a[j] = (mine && lane < kw && j < kw) ? B[lane + j * LD] : ((lane == j) ? cone<T>() : czero<T>());
+    T dinv[kStep];
     const R tiny2 = tiny * tiny;
 #pragma unroll
-    for (int t = 0; t < kSub; ++t) {
-        if (t < kw) {
-            T piv = shfl_c(a[t], t);
-            const R m2 = cabs2(piv);
-            if (!(m2 >= tiny2)) {  // lift (all lanes compute the same value)
-                const R am = sqrt(m2);
-                piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
-                if (lane == t) {
-                    a[t] = piv;
-                    atomicAdd(tiny_count, 1);
-                }
-            }
-            const T pinv = crecip_fast(piv);
-            if (lane == 0) dinv[t] = pinv;
-            const bool upd = row_lane && lane > t;
-            T l = cmul(a[t], pinv);
-            if (upd) a[t] = l;
-#pragma unroll
-            for (int c = t + 1; c < kSub; ++c) {
-                const T u = shfl_c(a[c], t);
-                if (upd) cmsub(a[c], l, u);
+    for (int k = 0; k < kStep; ++k) {
+        T piv = shfl_c(a[k], k);
+        if (!(cabs2(piv) >= tiny2)) {
+            const R am = sqrt(cabs2(piv));
+            piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
+            if (lane == k) {
+                a[k] = piv;
+                atomicAdd(tiny_count, 1);
             }
         }
-    }
-    if (row_lane)
+        dinv[k] = crecip_fast(piv);
+        const bool upd = mine && lane > k;
+        const T l = cmul(a[k], dinv[k]);
+        if (upd) a[k] = l;
 #pragma unroll
-        for (int c = 0; c < kSub; ++c)
-            if (c < kw) Ls[lane + c * kDiagLd] = a[c];
-    __syncwarp();
-    // lane q < 16: column q of inv(L) (x = e_q; x[i] -= L[i][t] x[t]);
-    // lane 16 + r: row r of inv(U) as column r of inv(U^T)
-    // (z = e_r; z[t] *= 1/U[t][t]; z[i] -= U[t][i] z[t]).
-    const bool upper = lane >= kSub;
-    const int q = lane & (kSub - 1);
-    const int si = upper ? kDiagLd : 1, st = upper ? 1 : kDiagLd;
-    T x[kSub];
-#pragma unroll
-    for (int i = 0; i < kSub; ++i) x[i] = (i == q) ? cone<T>() : czero<T>();
-#pragma unroll
-    for (int t = 0; t < kSub; ++t) {
-        if (t < kw && t >= q) {
-            if (upper) x[t] = cmul(x[t], dinv[t]);
-#pragma unroll
-            for (int i = t + 1; i < kSub; ++i)
-                if (i < kw) cmsub(x[i], Ls[i * si + t * st], x[t]);
+        for (int j = k + 1; j < kStep; ++j) {
+            const T u = shfl_c(a[j], k);
+            if (upd) cmsub(a[j], l, u);
         }
     }
-    if (q < kw) {
-        if (upper) {
+    // lane q: x = column q of inv(L) (x = e_q, x[i] -= L[i][t] x[t], L[i][t] in lane i)
+    //         y = row q of inv(U)    (y[c] = (delta_qc - sum_{q<=k<c} y[k] U[k][c]) / U[c][c], U[k][c] in lane k)
+    const int q = lane & (kStep - 1);
+    T x[kStep], y[kStep];
 #pragma unroll
-            for (int c = 0; c < kSub; ++c)
-                if (c >= q && c < kw) D[(c0 + q) + (c0 + c) * LD] = x[c];
-        } else {
+    for (int i = 0; i < kStep; ++i) x[i] = (i == q) ? cone<T>() : czero<T>();
 #pragma unroll
-            for (int i = 0; i < kSub; ++i)
-                if (i > q && i < kw) D[(c0 + i) + (c0 + q) * LD] = x[i];
+    for (int t = 0; t < kStep; ++t)
+#pragma unroll
+        for (int i = t + 1; i < kStep; ++i) {
+            const T lit = shfl_c(a[t], i);
+            if (t >= q) cmsub(x[i], lit, x[t]);
         }
+#pragma unroll
+    for (int c = 0; c < kStep; ++c) {
+        T s = (c == q) ? cone<T>() : czero<T>();
+#pragma unroll
+        for (int k = 0; k < c; ++k) {
+            const T ukc = shfl_c(a[c], k);
+            if (k >= q) cmsub(s, y[k], ukc);
+        }
+        y[c] = (c >= q) ? cmul(s, dinv[c]) : czero<T>();
+    }
+    if (mine && q < kw) {
+#pragma unroll
+        for (int i = 0; i < kStep; ++i)
+            if (i < kw) {
+                if (i > q) B[i + q * LD] = x[i];
+                if (i >= q) B[q + i * LD] = y[i];
+            }
     }
 }
 
 template <typename T, typename R>
-__global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 2 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
+__global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
                                                             int k0, int whole, R tiny, int *tiny_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *D = reinterpret_cast<T *>(smem_raw);
-    __shared__ T s_ls[kSub * kDiagLd];
-    __shared__ T s_dinv[kSub];
     const FrontD f = fr[f_begin + blockIdx.x];
     int n, P;
     T *G;
@@ -305,8 +299,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 2 : 1) k_dense
     }
     if (P <= 0 || n <= 0) return;
     const int64_t ld = f.ld;
-    const int S = (n + kSub - 1) / kSub * kSub, LD = S + 1, NBLK = S / kSub;
-    if (!whole) P = S;  // the identity border is factored along (no effect)
+    const int S = (n + 15) / 16 * 16, LD = S + 1, NBLK = S / 16;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int c = warp; c < S; c += kDenseThreads / 32)
         for (int r = lane; r < S; r += 32) {
@@ -319,144 +312,128 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 2 : 1) k_dense
     __syncthreads();
 
     const int tx = tid & 15, ty = tid >> 4;
-    for (int c0 = 0; c0 < P; c0 += kSub) {
-        const int kw = min(kSub, P - c0), b1 = c0 + kw;
-        if (warp == 0) warp_diag_block<T, R>(D, LD, c0, kw, tiny, tiny_count, s_ls, s_dinv);
+    for (int c0 = 0; c0 < P; c0 += kStep) {
+        const int kw = min(kStep, P - c0), b1 = c0 + kw;
+        if (warp == 0) lu4_inv_warp<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
         __syncthreads();
-        // L21 rows [b1, S): a[0:kw] <- a inv(U11);  U12 columns [b1, S): a <- inv(L11) a
+        // L21 rows [b1, S): l = a inv(U11);  U12 columns [b1, S): u = inv(L11) a
         const int nr = S - b1;
         for (int item = tid; item < 2 * nr; item += kDenseThreads) {
             const bool is_row = item < nr;
             const int idx = b1 + (is_row ? item : item - nr);
-            // element j of the row / column: D[base + j * step]
             T *base = is_row ? D + idx + c0 * LD : D + c0 + idx * LD;
             const int step = is_row ? LD : 1;
-            T v[kSub], o[kSub];
+            T v[kStep];
 #pragma unroll
-            for (int j = 0; j < kSub; ++j) v[j] = (j < kw) ? base[j * step] : czero<T>();
-            if (is_row) {
+            for (int j = 0; j < kStep; ++j) v[j] = (j < kw) ? base[j * step] : czero<T>();
 #pragma unroll
-                for (int c = 0; c < kSub; ++c) {
-                    T s = czero<T>();
+            for (int j = 0; j < kStep; ++j) {
+                T s = is_row ? czero<T>() : v[j];
 #pragma unroll
-                    for (int k = 0; k <= c; ++k)
-                        if (c < kw) cmac(s, v[k], D[(c0 + k) + (c0 + c) * LD]);
-                    o[c] = s;
+                for (int k = 0; k < kStep; ++k) {
+                    if (is_row && k <= j) cmac(s, v[k], D[(c0 + k) + (c0 + j) * LD]);
+                    if (!is_row && k < j) cmac(s, D[(c0 + j) + (c0 + k) * LD], v[k]);
                 }
-            } else {
-#pragma unroll
-                for (int i = 0; i < kSub; ++i) {
-                    T s = v[i];
-#pragma unroll
-                    for (int k = 0; k < i; ++k)
-                        if (i < kw) cmac(s, D[(c0 + i) + (c0 + k) * LD], v[k]);
-                    o[i] = s;
-                }
+                if (j < kw) base[j * step] = s;
             }
-#pragma unroll
-            for (int j = 0; j < kSub; ++j)
-                if (j < kw) base[j * step] = o[j];
         }
         __syncthreads();
-        // trailing rows/columns [b1, S) -= L21 U12 (rank kw)
-        const int Ilo = b1 / kSub;
+        // trailing rows / columns [b1, S) -= L21 U12 (rank kw)
+        const int Ilo = b1 / 16;
         for (int I0 = Ilo; I0 < NBLK; I0 += 4)
             for (int J0 = Ilo; J0 < NBLK; J0 += 4) {
-                T acc[4][4];
+                T l[4][kStep], u[kStep][4];
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (I0 + i < NBLK && J0 + j < NBLK)
-                            acc[i][j] = D[(kSub * (I0 + i) + tx) + (kSub * (J0 + j) + ty) * LD];
-#pragma unroll 4
-                for (int t = 0; t < kw; ++t) {
-                    T l[4], u[4];
+                    for (int k = 0; k < kStep; ++k)
+                        l[i][k] = (I0 + i < NBLK && k < kw) ? D[(16 * (I0 + i) + tx) + (c0 + k) * LD] : czero<T>();
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        if (I0 + i < NBLK) l[i] = D[(kSub * (I0 + i) + tx) + (c0 + t) * LD];
+                for (int k = 0; k < kStep; ++k)
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
-                        if (J0 + j < NBLK) u[j] = D[(c0 + t) + (kSub * (J0 + j) + ty) * LD];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-#pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            if (I0 + i < NBLK && J0 + j < NBLK) cmsub(acc[i][j], l[i], u[j]);
-                }
+                        u[k][j] = (J0 + j < NBLK && k < kw) ? D[(c0 + k) + (16 * (J0 + j) + ty) * LD] : czero<T>();
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (I0 + i < NBLK && J0 + j < NBLK && kSub * (I0 + i) + tx >= b1 &&
-                            kSub * (J0 + j) + ty >= b1)
-                            D[(kSub * (I0 + i) + tx) + (kSub * (J0 + j) + ty) * LD] = acc[i][j];
+                    for (int j = 0; j < 4; ++j) {
+                        const int r = 16 * (I0 + i) + tx, c = 16 * (J0 + j) + ty;
+                        if (I0 + i < NBLK && J0 + j < NBLK && r >= b1 && c >= b1) {
+                            T acc = D[r + c * LD];
+#pragma unroll
+                            for (int k = 0; k < kStep; ++k) cmsub(acc, l[i][k], u[k][j]);
+                            D[r + c * LD] = acc;
+                        }
+                    }
             }
         __syncthreads();
     }
 
-    // off-diagonal blocks of the inverses over the P x P pivot block, block
-    // row / column B from the ones before it (unit diagonal of inv(L) implied):
-    //   X[B, J] = -inv(L_BB) T,  T = sum_{K=J}^{B-1} L[B, K] X[K, J]
-    //   Y[J, B] = -T' inv(U_BB), T' = sum_{K=J}^{B-1} Y[J, K] U[K, B]
-    const int nbk = (P + kSub - 1) / kSub;
-    constexpr int kMaxB = kDenseMaxPiv / kSub - 1;  // 3
-    for (int B = 1; B < nbk; ++B) {
-        const int b0 = B * kSub, bs = min(kSub, P - b0);
-        T vl[kMaxB], vu[kMaxB];
+    // off-diagonal blocks of the inverses over the P x P pivot block, 4
+    // rows (columns) at a time.  Thread (col, quarter) of the lower part:
+    // T[i] = L[b0+i][col] + sum_{k in (col, b0), k = quarter mod 4} L[b0+i][k] X[k][col]
+    const int nb4 = (P + kStep - 1) / kStep;
+    const int q = tid & 3, g = tid >> 2;  // 64 groups of four threads
+    for (int B = 1; B < nb4; ++B) {
+        const int b0 = B * kStep, bs = min(kStep, P - b0);
+        T vl[kStep], vu[kStep];
+        // lower: groups g < b0 take column g; upper: groups g < b0 take row g
 #pragma unroll
-        for (int J = 0; J < kMaxB; ++J) {
-            if (J < B) {
-                const int j0 = J * kSub;
-                T sl = czero<T>(), su = czero<T>();
-                // K = J: X[J, J] unit lower (stored strictly below), Y[J, J] upper
+        for (int i = 0; i < kStep; ++i) vl[i] = vu[i] = czero<T>();
+        if (g < b0) {
+            const int col = g;
+            for (int k = col + 1 + q; k < b0; k += 4) {
+                const T x = D[k + col * LD];
 #pragma unroll
-                for (int k = 0; k < kSub; ++k) {
-                    const T xkj = (k == ty) ? cone<T>() : (k > ty ? D[(j0 + k) + (j0 + ty) * LD] : czero<T>());
-                    cmac(sl, D[(b0 + tx) + (j0 + k) * LD], xkj);
-                    if (k >= tx) cmac(su, D[(j0 + tx) + (j0 + k) * LD], D[(j0 + k) + (b0 + ty) * LD]);
-                }
-                for (int K = J + 1; K < B; ++K) {
-                    const int kk = K * kSub;
+                for (int i = 0; i < kStep; ++i) cmac(vl[i], D[(b0 + i) + k * LD], x);
+            }
+            const int row = g;
+            for (int k = row + q; k < b0; k += 4) {
+                const T y = D[row + k * LD];
 #pragma unroll
-                    for (int k = 0; k < kSub; ++k) {
-                        cmac(sl, D[(b0 + tx) + (kk + k) * LD], D[(kk + k) + (j0 + ty) * LD]);
-                        cmac(su, D[(j0 + tx) + (kk + k) * LD], D[(kk + k) + (b0 + ty) * LD]);
-                    }
-                }
-                vl[J] = sl;
-                vu[J] = su;
+                for (int j = 0; j < kStep; ++j) cmac(vu[j], y, D[k + (b0 + j) * LD]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kStep; ++i)
+            for (int off = 1; off < 4; off <<= 1) {
+                vl[i].x += __shfl_xor_sync(0xffffffffu, vl[i].x, off);
+                vl[i].y += __shfl_xor_sync(0xffffffffu, vl[i].y, off);
+                vu[i].x += __shfl_xor_sync(0xffffffffu, vu[i].x, off);
+                vu[i].y += __shfl_xor_sync(0xffffffffu, vu[i].y, off);
+            }
+        // X[B, col] = -inv(L_BB) (L[B, col] + sum), Y[row, B] = -(sum) inv(U_BB)
+        T xo[kStep], yo[kStep];
+        if (g < b0 && q == 0) {
+            const int col = g, row = g;
+#pragma unroll
+            for (int i = 0; i < kStep; ++i)
+                if (i < bs) vl[i] = cadd(vl[i], D[(b0 + i) + col * LD]);
+#pragma unroll
+            for (int i = 0; i < kStep; ++i) {
+                T s = vl[i];
+#pragma unroll
+                for (int k = 0; k < i; ++k) cmac(s, D[(b0 + i) + (b0 + k) * LD], vl[k]);
+                xo[i] = cmake<R>(-s.x, -s.y);
+            }
+#pragma unroll
+            for (int j = 0; j < kStep; ++j) {
+                T s = czero<T>();
+#pragma unroll
+                for (int k = 0; k <= j; ++k) cmac(s, vu[k], D[(b0 + k) + (b0 + j) * LD]);
+                yo[j] = cmake<R>(-s.x, -s.y);
             }
         }
         __syncthreads();
+        if (g < b0 && q == 0) {
+            const int col = g, row = g;
 #pragma unroll
-        for (int J = 0; J < kMaxB; ++J)
-            if (J < B) {
-                if (tx < bs) D[(b0 + tx) + (J * kSub + ty) * LD] = vl[J];
-                if (ty < bs) D[(J * kSub + tx) + (b0 + ty) * LD] = vu[J];
-            }
-        __syncthreads();
-#pragma unroll
-        for (int J = 0; J < kMaxB; ++J) {
-            if (J < B) {
-                const int j0 = J * kSub;
-                T sl = D[(b0 + tx) + (j0 + ty) * LD], su = czero<T>();
-#pragma unroll
-                for (int k = 0; k < kSub; ++k) {
-                    if (k < tx) cmac(sl, D[(b0 + tx) + (b0 + k) * LD], D[(b0 + k) + (j0 + ty) * LD]);
-                    if (k <= ty && k < bs) cmac(su, D[(j0 + tx) + (b0 + k) * LD], D[(b0 + k) + (b0 + ty) * LD]);
+            for (int i = 0; i < kStep; ++i)
+                if (i < bs) {
+                    D[(b0 + i) + col * LD] = xo[i];
+                    D[row + (b0 + i) * LD] = yo[i];
                 }
-                vl[J] = cmake<R>(-sl.x, -sl.y);
-                vu[J] = cmake<R>(-su.x, -su.y);
-            }
         }
-        __syncthreads();
-#pragma unroll
-        for (int J = 0; J < kMaxB; ++J)
-            if (J < B) {
-                if (tx < bs) D[(b0 + tx) + (J * kSub + ty) * LD] = vl[J];
-                if (ty < bs) D[(J * kSub + tx) + (b0 + ty) * LD] = vu[J];
-            }
         __syncthreads();
     }
     for (int c = warp; c < n; c += kDenseThreads / 32)
@@ -601,6 +578,124 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
             for (int a = threadIdx.x; a < mu; a += blockDim.x) w[rm[a]] = cadd(w[rm[a]], wc[a]);
         }
         __syncthreads();
+    }
+}
+
+// ---- substitutions of levels whose fronts have at most 64 pivots --------------
+// One CTA per front does the whole step of a direction (the gather, the
+// triangular product with the stored inverse and the update rows), instead
+// of a gather launch plus one launch per panel.  Rows of the column-major
+// front go to consecutive lanes, so every product streams the front down
+// its columns; the four thread groups split a sum by column and meet in
+// shared memory.
+constexpr int kSmallThreads = 256;
+constexpr int kSmallMaxM = 2048;  // fronts up to this size use the one-launch steps
+constexpr size_t kSmallSmemMax = 200 * 1024;
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t small_smem_bytes(int nrhs, int maxm) {
+    return ((size_t)nrhs * maxm + 4 * 64) * sizeof(T);
+}
+
+// sum over t in [t_lo, t_hi) of F[row, t] v[t], the range split over the four
+// groups (t = g mod 4); returns the total in group 0 (row < 64).
+template <typename T>
+__device__ __forceinline__ T split_rowdot(const T *F, int64_t ld, int row, bool live, int t_lo, int t_hi,
+                                          const T *v, T *part) {
+    const int g = threadIdx.x >> 6, rr = threadIdx.x & 63;
+    T s = czero<T>();
+    if (live)
+        for (int t = t_lo + g; t < t_hi; t += 4) cmac(s, F[row + (int64_t)t * ld], v[t]);
+    part[g * 64 + rr] = s;
+    __syncthreads();
+    T tot = czero<T>();
+    if (g == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) tot = cadd(tot, part[q * 64 + rr]);
+    }
+    __syncthreads();
+    return tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads)
+    k_fwd_small(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+                const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
+                int nrhs, int f_begin, int maxm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *ws = reinterpret_cast<T *>(smem_raw);  // [rhs][maxm]
+    T *part = ws + (size_t)nrhs * maxm;        // [4][64]
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int32_t *v = vars + f.voff;
+    const int tid = threadIdx.x;
+    for (int r = 0; r < nrhs; ++r)
+        for (int k = tid; k < f.m; k += blockDim.x)
+            ws[r * maxm + k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+    __syncthreads();
+    for (int slot = 0; slot < 2; ++slot) {
+        const int c = slot ? f.c1 : f.c0;
+        if (c < 0) continue;
+        const FrontD ch = fr[c];
+        const int mu = ch.m - ch.p;
+        const int32_t *rm = relmap + ch.voff + ch.p;
+        for (int r = 0; r < nrhs; ++r) {
+            const T *wc = W + r * sum_m + ch.voff + ch.p;
+            for (int a = tid; a < mu; a += blockDim.x) ws[r * maxm + rm[a]] = cadd(ws[r * maxm + rm[a]], wc[a]);
+        }
+        __syncthreads();
+    }
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int rr = tid & 63;
+    // y = inv(L11) w_P (unit diagonal): y_r = w_r + sum_{t<r} invL[r][t] w_t
+    for (int r = 0; r < nrhs; ++r) {
+        T *w = ws + r * maxm;
+        const T s = split_rowdot(F, ld, rr, rr < f.p, 0, rr, w, part);
+        T y = czero<T>();
+        if (tid < f.p) {
+            y = cadd(w[tid], s);
+            Y[r * sum_m + f.voff + tid] = y;
+        }
+        __syncthreads();  // every thread has read w[0:p]
+        if (tid < f.p) w[tid] = y;
+        __syncthreads();
+    }
+    // w_B -= L21 y, one thread per update row
+    for (int r = 0; r < nrhs; ++r) {
+        const T *y = ws + r * maxm;
+        for (int row = f.p + tid; row < f.m; row += blockDim.x) {
+            T s = y[row];
+            for (int t = 0; t < f.p; ++t) cmsub(s, F[row + (int64_t)t * ld], y[t]);
+            W[r * sum_m + f.voff + row] = s;
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kSmallThreads)
+    k_bwd_small(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const T *__restrict__ pool,
+                const T *__restrict__ Y, double2 *x, int64_t sum_m, int64_t n, int nrhs, int f_begin, int maxm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);  // [rhs][maxm]: pivots then x_B
+    T *part = xs + (size_t)nrhs * maxm;
+    const FrontD f = fr[f_begin + blockIdx.x];
+    const int32_t *v = vars + f.voff;
+    const int tid = threadIdx.x;
+    for (int r = 0; r < nrhs; ++r)
+        for (int k = f.p + tid; k < f.m; k += blockDim.x) xs[r * maxm + k] = from_c128<T>(x[r * n + v[k]], 1.0);
+    __syncthreads();
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int rr = tid & 63;
+    for (int r = 0; r < nrhs; ++r) {
+        T *xr = xs + r * maxm;
+        // acc = y - U12 x_B
+        const T s = split_rowdot(F, ld, rr, rr < f.p, f.p, f.m, xr, part);
+        if (tid < f.p) xr[tid] = csub(Y[r * sum_m + f.voff + tid], s);
+        __syncthreads();
+        // x_P = inv(U11) acc: x_r = sum_{t>=r} invU[r][t] acc_t
+        const T xv = split_rowdot(F, ld, rr, rr < f.p, rr, f.p, xr, part);
+        if (tid < f.p) x[r * n + v[tid]] = to_c128(xv, 1.0);
     }
 }
 
@@ -1483,11 +1578,20 @@ int set_smem_attrs() {
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
     return FDFD_OK;
 }
 
 // x = A^-1 b for nrhs columns (b, x complex128 on device; may alias d_tmp).
 // s_in / s_out are device arrays of per-column scales.
+// Levels whose fronts all have at most 64 pivots take the one-launch steps
+// of each direction when their vectors fit in shared memory.
+template <typename T>
+bool small_level_fits(int maxp, int maxm, int nrhs) {
+    return maxp <= NB && maxm <= kSmallMaxM && small_smem_bytes<T>(nrhs, maxm) <= kSmallSmemMax;
+}
+
 // Epoch of the next cooperative launch (never 0, the value flags start at).
 inline unsigned next_epoch(fdfd_factor *fac) {
     if (++fac->epoch == 0) ++fac->epoch;
@@ -1527,9 +1631,15 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
+        const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
+        if (small_level_fits<T>(maxp, maxm, nrhs)) {
+            k_fwd_small<T><<<nfl, kSmallThreads, small_smem_bytes<T>(nrhs, maxm), st>>>(
+                fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, maxm);
+            prof_end(PROF_SOLVE_FWD, st, 1);
+            continue;
+        }
         k_fwd_gather<T><<<nfl, 256, 0, st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, b, fac->d_unit,
                                              W, sum_m, n, nrhs, fb);
-        const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         int nl = 1;
         for (int k0 = 0; k0 < maxp; k0 += NB, ++nl) {
             const int rows = std::max(1, (maxm - k0 + kItemRows - 1) / kItemRows);
@@ -1564,6 +1674,13 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             const int grid = std::max(1, std::min(fac->coop_grid, items));
             CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
+            prof_end(PROF_SOLVE_BWD, st, 1);
+            continue;
+        }
+        if (small_level_fits<T>(maxp, S.lev_max_m[L], nrhs)) {
+            const int maxm = S.lev_max_m[L];
+            k_bwd_small<T><<<nfl, kSmallThreads, small_smem_bytes<T>(nrhs, maxm), st>>>(
+                fac->d_fronts, fac->d_vars, pool, Y, x, sum_m, n, nrhs, fb, maxm);
             prof_end(PROF_SOLVE_BWD, st, 1);
             continue;
         }
@@ -1725,7 +1842,7 @@ int64_t bwd_layout(const Symbolic &S, int max_nrhs, std::vector<char> *wide, std
 // Levels with at least kCoopPanels panel steps run their substitutions as
 // cooperative launches; their opener scratch (per front: column blocks x
 // rhs x p) is laid out here.
-constexpr int kCoopPanels = 4;
+constexpr int kCoopPanels = 2;
 int64_t coop_layout(const Symbolic &S, int max_nrhs, std::vector<char> *lev, std::vector<int64_t> *off) {
     int64_t best = 0;
     if (lev) lev->assign(S.nlev, 0);
