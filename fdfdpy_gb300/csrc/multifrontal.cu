@@ -160,7 +160,7 @@ __global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__res
 //              and the update matrix come out of the same launch (small
 //              fronts, where four launches per level would each re-read the
 //              front).
-// Right-looking in steps of 4 pivots: one warp factors and inverts the
+// Right-looking in steps of 4 pivots: one thread factors and inverts the
 // 4 x 4 diagonal block in registers, one thread per row / column forms
 // L21 = A21 inv(U11) and U12 = inv(L11) A12, and all threads apply the
 // rank-4 update with 4 x 4 register tiles.  The loop bodies are small and
@@ -204,84 +204,68 @@ __device__ __forceinline__ void cp_async_elem(T *dst_smem, const T *src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <typename T>
-__device__ __forceinline__ T shfl_c(T v, int src) {
-    v.x = __shfl_sync(0xffffffffu, v.x, src);
-    v.y = __shfl_sync(0xffffffffu, v.y, src);
-    return v;
-}
-
-// Warp 0: LU (no pivoting; a pivot below `tiny` in modulus is lifted and
-// counted) of the kw x kw block at B (leading dimension LD), then inv(L)
-// strictly below and inv(U) on and above the diagonal, in place.  Lane i < 4
-// holds row i; the pivot row travels by shuffles; lane q then forms column q
-// of inv(L) and row q of inv(U).
+// One thread: LU (no pivoting; a pivot below `tiny` in modulus is lifted
+// and counted) of the kw x kw block at B (leading dimension LD), then
+// inv(L) strictly below and inv(U) on and above the diagonal, in place.
 template <typename T, typename R>
-__device__ __forceinline__ void lu4_inv_warp(T *B, int LD, int kw, R tiny, int *tiny_count) {
-    const int lane = threadIdx.x & 31;
-    const bool mine = lane < kStep;
-    T a[kStep];
+__device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_count) {
+    T a[kStep][kStep];
 #pragma unroll
-    for (int j = 0; j < kStep; ++j)
-        a[j] = (mine && lane < kw && j < kw) ? B[lane + j * LD] : ((lane == j) ? cone<T>() : czero<T>());
+    for (int i = 0; i < kStep; ++i)
+#pragma unroll
+        for (int j = 0; j < kStep; ++j)
+            a[i][j] = (i < kw && j < kw) ? B[i + j * LD] : (i == j ? cone<T>() : czero<T>());
     T dinv[kStep];
     const R tiny2 = tiny * tiny;
 #pragma unroll
     for (int k = 0; k < kStep; ++k) {
-        T piv = shfl_c(a[k], k);
-        if (!(cabs2(piv) >= tiny2)) {
-            const R am = sqrt(cabs2(piv));
-            piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
-            if (lane == k) {
-                a[k] = piv;
-                atomicAdd(tiny_count, 1);
+        if (!(cabs2(a[k][k]) >= tiny2)) {
+            const R am = sqrt(cabs2(a[k][k]));
+            a[k][k] = (am > R(0)) ? cmake<R>(a[k][k].x / am * tiny, a[k][k].y / am * tiny) : cmake<R>(tiny, R(0));
+            atomicAdd(tiny_count, 1);
+        }
+        dinv[k] = crecip_fast(a[k][k]);
+#pragma unroll
+        for (int i = k + 1; i < kStep; ++i) {
+            a[i][k] = cmul(a[i][k], dinv[k]);
+#pragma unroll
+            for (int j = k + 1; j < kStep; ++j) cmsub(a[i][j], a[i][k], a[k][j]);
+        }
+    }
+    // inv(L): column q, x = e_q, x[i] -= L[i][t] x[t]
+    T li[kStep][kStep], ui[kStep][kStep];
+#pragma unroll
+    for (int q = 0; q < kStep; ++q) {
+#pragma unroll
+        for (int i = 0; i < kStep; ++i) li[i][q] = (i == q) ? cone<T>() : czero<T>();
+#pragma unroll
+        for (int t = q; t < kStep; ++t)
+#pragma unroll
+            for (int i = t + 1; i < kStep; ++i) cmsub(li[i][q], a[i][t], li[t][q]);
+    }
+    // inv(U): row r, y[c] = (delta_rc - sum_{r<=k<c} y[k] U[k][c]) / U[c][c]
+#pragma unroll
+    for (int r = 0; r < kStep; ++r)
+#pragma unroll
+        for (int c = 0; c < kStep; ++c) {
+            if (c < r) {
+                ui[r][c] = czero<T>();
+            } else {
+                T s = (c == r) ? cone<T>() : czero<T>();
+#pragma unroll
+                for (int k = r; k < c; ++k) cmsub(s, ui[r][k], a[k][c]);
+                ui[r][c] = cmul(s, dinv[c]);
             }
         }
-        dinv[k] = crecip_fast(piv);
-        const bool upd = mine && lane > k;
-        const T l = cmul(a[k], dinv[k]);
-        if (upd) a[k] = l;
 #pragma unroll
-        for (int j = k + 1; j < kStep; ++j) {
-            const T u = shfl_c(a[j], k);
-            if (upd) cmsub(a[j], l, u);
-        }
-    }
-    // lane q: x = column q of inv(L) (x = e_q, x[i] -= L[i][t] x[t], L[i][t] in lane i)
-    //         y = row q of inv(U)    (y[c] = (delta_qc - sum_{q<=k<c} y[k] U[k][c]) / U[c][c], U[k][c] in lane k)
-    const int q = lane & (kStep - 1);
-    T x[kStep], y[kStep];
+    for (int i = 0; i < kStep; ++i)
 #pragma unroll
-    for (int i = 0; i < kStep; ++i) x[i] = (i == q) ? cone<T>() : czero<T>();
-#pragma unroll
-    for (int t = 0; t < kStep; ++t)
-#pragma unroll
-        for (int i = t + 1; i < kStep; ++i) {
-            const T lit = shfl_c(a[t], i);
-            if (t >= q) cmsub(x[i], lit, x[t]);
-        }
-#pragma unroll
-    for (int c = 0; c < kStep; ++c) {
-        T s = (c == q) ? cone<T>() : czero<T>();
-#pragma unroll
-        for (int k = 0; k < c; ++k) {
-            const T ukc = shfl_c(a[c], k);
-            if (k >= q) cmsub(s, y[k], ukc);
-        }
-        y[c] = (c >= q) ? cmul(s, dinv[c]) : czero<T>();
-    }
-    if (mine && q < kw) {
-#pragma unroll
-        for (int i = 0; i < kStep; ++i)
-            if (i < kw) {
-                if (i > q) B[i + q * LD] = x[i];
-                if (i >= q) B[q + i * LD] = y[i];
-            }
-    }
+        for (int j = 0; j < kStep; ++j)
+            if (i < kw && j < kw) B[i + j * LD] = (i > j) ? li[i][j] : ui[i][j];
 }
 
 template <typename T, typename R>
-__global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
+__global__ void __launch_bounds__(kDenseThreads) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
                                                             int k0, int whole, R tiny, int *tiny_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *D = reinterpret_cast<T *>(smem_raw);
@@ -314,7 +298,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     const int tx = tid & 15, ty = tid >> 4;
     for (int c0 = 0; c0 < P; c0 += kStep) {
         const int kw = min(kStep, P - c0), b1 = c0 + kw;
-        if (warp == 0) lu4_inv_warp<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
+        if (tid == 0) lu4_inv<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
         __syncthreads();
         // L21 rows [b1, S): l = a inv(U11);  U12 columns [b1, S): u = inv(L11) a
         const int nr = S - b1;
@@ -450,10 +434,8 @@ enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
 // In the in-place modes a CTA owns complete rows (TRSM_L) or columns
 // (TRSM_U) of its output and reads all of them before writing.
 template <typename T, typename R, int MODE>
-__global__ void __launch_bounds__(256) k_gemm(const FrontD *__restrict__ fr, T *pool, int f_begin,
-                                              int k0) {
-    __shared__ T As[BK][BM + 1];
-    __shared__ T Bs[BK][BN + 1];
+__device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, int ytile,
+                                          int ztile, T (*As)[BM + 1], T (*Bs)[BN + 1]) {
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
@@ -461,11 +443,11 @@ __global__ void __launch_bounds__(256) k_gemm(const FrontD *__restrict__ fr, T *
     const int m = f.m;
     int rbase, cbase, rend, cend;
     if (MODE == SCHUR) {
-        rbase = t0 + blockIdx.y * BM; cbase = t0 + blockIdx.z * BN; rend = m; cend = m;
+        rbase = t0 + ytile * BM; cbase = t0 + ztile * BN; rend = m; cend = m;
     } else if (MODE == TRSM_L) {
-        rbase = t0 + blockIdx.y * BM; cbase = k0; rend = m; cend = t0;
+        rbase = t0 + ytile * BM; cbase = k0; rend = m; cend = t0;
     } else {
-        rbase = k0; cbase = t0 + blockIdx.z * BN; rend = t0; cend = m;
+        rbase = k0; cbase = t0 + ztile * BN; rend = t0; cend = m;
     }
     if (rbase >= rend || cbase >= cend) return;
     T *F = pool + f.f_off;
@@ -545,6 +527,26 @@ __global__ void __launch_bounds__(256) k_gemm(const FrontD *__restrict__ fr, T *
             else dst = acc[qa][qb];
         }
     }
+}
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0) {
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+    gemm_tile<T, R, SCHUR>(fr, pool, f_begin, k0, blockIdx.y, blockIdx.z, As, Bs);
+}
+
+// Both triangular updates of a panel step in one launch: blockIdx.z = 0
+// forms L (row tile blockIdx.y), blockIdx.z = 1 forms U (column tile
+// blockIdx.y).
+template <typename T, typename R>
+__global__ void __launch_bounds__(256) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0) {
+    __shared__ T As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+    if (blockIdx.z == 0)
+        gemm_tile<T, R, TRSM_L>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
+    else
+        gemm_tile<T, R, TRSM_U>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs);
 }
 
 // ---- solve ------------------------------------------------------------------
@@ -1215,17 +1217,16 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             if (trail <= 0) continue;
             const int tiles = (trail + BM - 1) / BM;
             prof_begin(PROF_TRSM, st);
-            k_gemm<T, R, TRSM_L><<<dim3(nfl, tiles, 1), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
-            k_gemm<T, R, TRSM_U><<<dim3(nfl, 1, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
-            prof_end(PROF_TRSM, st, 2);
+            k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+            prof_end(PROF_TRSM, st, 1);
             prof_begin(PROF_SCHUR, st);
             if (std::is_same<T, c64>::value && fac->use_tc && fac->tc_level[L]) {
                 int rc = tc_schur_step(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch,
                                        fac->d_tcerr, st);
                 if (rc) return rc;
-                prof_end(PROF_SCHUR, st, 3);
+                prof_end(PROF_SCHUR, st, 2);
             } else {
-                k_gemm<T, R, SCHUR><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+                k_schur_simt<T, R><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
                 prof_end(PROF_SCHUR, st, 1);
             }
         }

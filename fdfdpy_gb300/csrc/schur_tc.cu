@@ -14,17 +14,20 @@
 // split (x = hi + lo, both TF32; A B ~ Ahi Bhi + Ahi Blo + Alo Bhi), the
 // three MMAs accumulating in FP32 in tensor memory.
 //
-// Data movement: a pack kernel writes each 128-row A' tile and each
-// 64-column B'' tile (hi and lo) contiguously in global scratch in the
-// canonical no-swizzle K-major core-matrix layout of tcgen05 (8 rows x 16
-// bytes per core matrix); the GEMM CTA pulls them into shared memory with
-// four bulk copies (cp.async.bulk, completion on an mbarrier), one thread
-// issues the 48 tcgen05.mma of the tile (16 K-steps x 3), tcgen05.commit
-// signals a second mbarrier, and four warps read the 128 x 64 FP32
-// accumulator back with tcgen05.ld (each warp its 32 TMEM lanes) and apply
-// C -= acc with coalesced column-major stores.  All waits are bounded:
-// on time-out the CTA records an error code, waits (bounded) for its own
-// operations, frees its tensor memory and returns.
+// Data movement: the GEMM CTA's four epilogue warps first write the A'
+// rows of their 128-row tile (hi and lo, straight from the front) into
+// tensor memory, one TMEM lane per row, so the MMAs read A from TMEM; a
+// pack kernel writes each 32-column B'' tile (hi and lo) contiguously in
+// global scratch in the canonical no-swizzle K-major core-matrix layout
+// (8 rows x 16 bytes per core matrix), and a producer thread streams them
+// into shared memory with bulk copies (cp.async.bulk, completion on an
+// mbarrier per stage); one thread issues the 48 tcgen05.mma of a tile
+// (16 K-steps x 3), tcgen05.commit signals the epilogue and releases the
+// stage, and the four warps read the 128 x 64 FP32 accumulator back with
+// tcgen05.ld (each warp its 32 TMEM lanes) and apply C -= acc with
+// coalesced column-major stores.  All waits are bounded: on time-out the
+// CTA records an error code, waits (bounded) for its own operations, frees
+// its tensor memory and returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -97,6 +100,33 @@ __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+// A from tensor memory (a_tmem: lane = row, one TF32 element per column),
+// B from shared memory.
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// 32 consecutive 32-bit columns of this thread's TMEM lane (warp w may
+// address lanes 32 (w % 4) .. + 31).
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+        : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() {
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                      smem_u32(bar))
@@ -145,32 +175,6 @@ __device__ __forceinline__ uint32_t pack_off(int r, int k, int groups) {
     return (uint32_t)(s * (2 * groups * 128) + ki * (groups * 128) + mi * 128 + rr * 16 + e * 4);
 }
 
-// A' tiles of every front of a level: grid (front, row tile), 256 threads.
-__global__ void k_pack_a(const TcFront *__restrict__ fr, const c64 *__restrict__ pool, int f_begin, int k0,
-                         uint8_t *scratch) {
-    const TcFront f = fr[f_begin + blockIdx.x];
-    const int w = min(kPanel, f.p - k0);
-    if (w <= 0) return;
-    const int t0 = k0 + w, mt = f.m - t0;
-    const int rt = blockIdx.y;
-    if (rt * kTileM >= mt) return;
-    uint8_t *hi = scratch + f.a_off + (size_t)rt * 2 * kATileBytes;
-    uint8_t *lo = hi + kATileBytes;
-    const c64 *F = pool + f.f_off;
-    for (int idx = threadIdx.x; idx < kTileM * kPanel; idx += blockDim.x) {
-        const int r = idx % kTileM, l = idx / kTileM;
-        const int row = t0 + rt * kTileM + r;
-        c64 v = czero<c64>();
-        if (row < f.m && l < w) v = F[row + (int64_t)(k0 + l) * f.ld];
-        const float h0 = to_tf32(v.x), h1 = to_tf32(v.y);
-        const uint32_t o0 = pack_off(r, 2 * l, kTileM / 8), o1 = pack_off(r, 2 * l + 1, kTileM / 8);
-        *(float *)(hi + o0) = h0;
-        *(float *)(hi + o1) = h1;
-        *(float *)(lo + o0) = to_tf32(v.x - h0);
-        *(float *)(lo + o1) = to_tf32(v.y - h1);
-    }
-}
-
 // B'' tiles: grid (front, column tile), 256 threads.
 __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__ pool, int f_begin, int k0,
                          uint8_t *scratch) {
@@ -206,17 +210,30 @@ __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__
 }
 
 // ---- the GEMM ------------------------------------------------------------------
-// One CTA = one 128-row tile of C and up to kColTilesPerCta 32-column tiles.
-// Warp 4 (lane 0) is the control thread: it pulls the A tile (hi, lo) once,
-// then for each column tile pulls B (hi, lo) into the single B buffer once
-// the previous tile's MMAs have released it, and issues 48 MMAs into one of
-// two TMEM accumulators.  Warps 0-3 drain the other accumulator meanwhile
-// (tcgen05.ld of their 32 TMEM lanes, C -= acc) and hand it back through an
-// mbarrier.  Every wait is bounded.
+// One CTA = one 128-row tile of C and up to kColTilesPerCta 32-column tiles,
+// warp-specialized:
+//   warps 0-3 first write the tile's A' rows (hi and lo TF32 parts of the L
+//     panel, read straight from the front) into tensor memory -- thread =
+//     TMEM lane = row -- so the MMAs read A from TMEM and only B from shared
+//     memory; then they drain the accumulators (tcgen05.ld of their 32 TMEM
+//     lanes, C -= acc), the next tile's C entries already loading;
+//   warp 5 (lane 0) streams the B'' tiles (hi, lo) through kStages shared-
+//     memory stages, refilling a stage once the MMAs that read it are done;
+//   warp 4 (lane 0) issues the 48 MMAs of each column tile (16 K-steps x 3)
+//     into one of two TMEM accumulators and commits them to the epilogue's
+//     barrier and to the stage's release barrier.
+// TMEM columns: A hi [0,128), A lo [128,256), accumulators [256,384).
+// Every wait is bounded; on time-out a thread records an error, the
+// producer waits (bounded) for the copies it issued, and the CTA frees its
+// tensor memory and returns.
 constexpr int kColTilesPerCta = 8;
-constexpr uint32_t kSmemBytes = 2 * kATileBytes + 2 * kBTileBytes + 256;
+constexpr int kStages = 3;
+constexpr uint32_t kStageBytes = 2 * kBTileBytes;
+constexpr uint32_t kSmemBytes = kStages * kStageBytes + 256;
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kCtaThreads = 160;
+constexpr int kCtaThreads = 192;
+constexpr uint32_t kTmemAlloc = 512;
+constexpr uint32_t kTmemAHi = 0, kTmemALo = 2 * kPanel, kTmemAcc = 4 * kPanel;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -236,16 +253,19 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
     if (rt * kTileM >= mt || ct0 >= cts) return;
     const int J = min(kColTilesPerCta, cts - ct0);
 
-    uint8_t *a_hi = smem, *a_lo = smem + kATileBytes;
-    uint8_t *b_hi = smem + 2 * kATileBytes, *b_lo = b_hi + kBTileBytes;
-    uint64_t *bars = (uint64_t *)(smem + 2 * kATileBytes + 2 * kBTileBytes);
-    uint64_t *bar_a = &bars[0], *bar_b = &bars[1], *bar_mma = &bars[2], *bar_epi = &bars[4];
-    uint32_t *tmem_slot = (uint32_t *)(bars + 6);
+    uint8_t *b_base = smem;
+    uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
+    uint64_t *bar_a = &bars[0], *bar_full = &bars[1], *bar_free = &bars[1 + kStages];
+    uint64_t *bar_mma = &bars[1 + 2 * kStages], *bar_epi = &bars[3 + 2 * kStages];
+    uint32_t *tmem_slot = (uint32_t *)(bars + 5 + 2 * kStages);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(bar_a, 1);
-        mbar_init(bar_b, 1);
+        mbar_init(bar_a, 4);
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&bar_full[s], 1);
+            mbar_init(&bar_free[s], 1);
+        }
         mbar_init(&bar_mma[0], 1);
         mbar_init(&bar_mma[1], 1);
         mbar_init(&bar_epi[0], 4);
@@ -253,7 +273,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 4) {
-        tmem_alloc(tmem_slot, 2 * kTmemCols);
+        tmem_alloc(tmem_slot, kTmemAlloc);
         tmem_relinquish();
     }
     tc_fence_before();
@@ -261,64 +281,105 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 4) {
+    if (warp == 5) {
         if (lane == 0) {
             bool ok = true;
-            const uint8_t *ga = scratch + f.a_off + (size_t)rt * 2 * kATileBytes;
-            mbar_arrive_expect_tx(bar_a, 2 * kATileBytes);
-            bulk_g2s(a_hi, ga, kATileBytes, bar_a);
-            bulk_g2s(a_lo, ga + kATileBytes, kATileBytes, bar_a);
-            ok = mbar_wait_bounded(bar_a, 0, kWaitLimit);
-            constexpr uint32_t idesc = idesc_tf32(kTileM, 2 * kTileNc);
-            constexpr uint32_t a_step = 2 * (kTileM / 8) * 128;
-            constexpr uint32_t b_step = 2 * (2 * kTileNc / 8) * 128;
-            const uint32_t sa_hi = smem_u32(a_hi), sa_lo = smem_u32(a_lo);
-            const uint32_t sb_hi = smem_u32(b_hi), sb_lo = smem_u32(b_lo);
-            for (int j = 0; j < J && ok; ++j) {
-                const int sidx = j & 1;
-                if (j >= 1 && !mbar_wait_bounded(&bar_mma[(j - 1) & 1], ((j - 1) >> 1) & 1, kWaitLimit)) {
-                    ok = false;  // B buffer still in use
+            int issued = 0;
+            for (int j = 0; j < J; ++j) {
+                const int s = j % kStages;
+                if (j >= kStages && !mbar_wait_bounded(&bar_free[s], ((j / kStages) - 1) & 1, kWaitLimit)) {
+                    ok = false;
                     break;
                 }
                 const uint8_t *gb = scratch + f.b_off + (size_t)(ct0 + j) * 2 * kBTileBytes;
-                mbar_arrive_expect_tx(bar_b, 2 * kBTileBytes);
-                bulk_g2s(b_hi, gb, kBTileBytes, bar_b);
-                bulk_g2s(b_lo, gb + kBTileBytes, kBTileBytes, bar_b);
-                if (!mbar_wait_bounded(bar_b, j & 1, kWaitLimit)) { ok = false; break; }
+                uint8_t *sb = b_base + s * kStageBytes;
+                mbar_arrive_expect_tx(&bar_full[s], kStageBytes);
+                bulk_g2s(sb, gb, kBTileBytes, &bar_full[s]);
+                bulk_g2s(sb + kBTileBytes, gb + kBTileBytes, kBTileBytes, &bar_full[s]);
+                issued = j + 1;
+            }
+            // the copies this thread issued complete before the CTA exits
+            for (int j = (issued > kStages ? issued - kStages : 0); j < issued; ++j)
+                mbar_wait_bounded(&bar_full[j % kStages], (j / kStages) & 1, kWaitLimit);
+            if (!ok) atomicExch(err, 3);
+        }
+    } else if (warp == 4) {
+        if (lane == 0) {
+            bool ok = mbar_wait_bounded(bar_a, 0, kWaitLimit);
+            constexpr uint32_t idesc = idesc_tf32(kTileM, 2 * kTileNc);
+            constexpr uint64_t b_step = (2 * (2 * kTileNc / 8) * 128) >> 4;
+            const uint64_t bh00 = smem_desc(smem_u32(b_base), (2 * kTileNc / 8) * 128, 128);
+            tc_fence_after();
+            for (int j = 0; j < J && ok; ++j) {
+                const int s = j % kStages, sidx = j & 1;
+                if (!mbar_wait_bounded(&bar_full[s], (j / kStages) & 1, kWaitLimit)) { ok = false; break; }
                 if (j >= 2 && !mbar_wait_bounded(&bar_epi[sidx], ((j - 2) >> 1) & 1, kWaitLimit)) {
                     ok = false;  // accumulator still being drained
                     break;
                 }
                 tc_fence_after();
-                const uint32_t d = tmem + (uint32_t)(sidx * kTmemCols);
+                const uint64_t bh0 = bh00 + (uint64_t)((s * kStageBytes) >> 4);
+                const uint64_t bl0 = bh0 + (uint64_t)(kBTileBytes >> 4);
+                const uint32_t d = tmem + kTmemAcc + (uint32_t)(sidx * kTmemCols);
+#pragma unroll
                 for (int s2 = 0; s2 < 2 * kPanel / 8; ++s2) {
-                    const uint64_t ah = smem_desc(sa_hi + s2 * a_step, (kTileM / 8) * 128, 128);
-                    const uint64_t al = smem_desc(sa_lo + s2 * a_step, (kTileM / 8) * 128, 128);
-                    const uint64_t bh = smem_desc(sb_hi + s2 * b_step, (2 * kTileNc / 8) * 128, 128);
-                    const uint64_t bl = smem_desc(sb_lo + s2 * b_step, (2 * kTileNc / 8) * 128, 128);
-                    mma_tf32(d, ah, bh, idesc, s2 > 0 ? 1u : 0u);
-                    mma_tf32(d, ah, bl, idesc, 1);
-                    mma_tf32(d, al, bh, idesc, 1);
+                    const uint32_t ah = tmem + kTmemAHi + 8 * s2, al = tmem + kTmemALo + 8 * s2;
+                    mma_tf32_ts(d, ah, bh0 + s2 * b_step, idesc, s2 > 0 ? 1u : 0u);
+                    mma_tf32_ts(d, ah, bl0 + s2 * b_step, idesc, 1);
+                    mma_tf32_ts(d, al, bh0 + s2 * b_step, idesc, 1);
                 }
                 mma_commit(&bar_mma[sidx]);
+                mma_commit(&bar_free[s]);
             }
             if (!ok) atomicExch(err, 1);
         }
     } else {
-        // epilogue warps 0-3: warp w owns TMEM lanes (accumulator rows) 32w..32w+31
+        // warps 0-3: warp w owns TMEM lanes (tile rows) 32w..32w+31
         const int row = t0 + rt * kTileM + warp * 32 + lane;
+        const bool live = row < f.m;
         c64 *F = pool + f.f_off;
         const int64_t ld = f.ld;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        // A' row: (Re, Im) of L[row, k0 + l] at columns (2l, 2l + 1), hi and lo parts
+#pragma unroll 1
+        for (int c = 0; c < 2 * kPanel / 32; ++c) {
+            uint32_t hi[32], lo[32];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int l = 16 * c + q;
+                c64 v = czero<c64>();
+                if (live && l < w) v = F[row + (int64_t)(k0 + l) * ld];
+                const float hx = to_tf32(v.x), hy = to_tf32(v.y);
+                hi[2 * q] = __float_as_uint(hx);
+                hi[2 * q + 1] = __float_as_uint(hy);
+                lo[2 * q] = __float_as_uint(to_tf32(v.x - hx));
+                lo[2 * q + 1] = __float_as_uint(to_tf32(v.y - hy));
+            }
+            tmem_st32(lane_base + kTmemAHi + 32 * c, hi);
+            tmem_st32(lane_base + kTmemALo + 32 * c, lo);
+        }
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar_a);
+
+        c64 cv[kTileNc], nv[kTileNc];
+#pragma unroll
+        for (int q = 0; q < kTileNc; ++q) {
+            const int col = t0 + ct0 * kTileNc + q;
+            cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+            nv[q] = czero<c64>();
+        }
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
             const int colbase = t0 + (ct0 + j) * kTileNc;
-            // prefetch this row's 32 C entries of the tile while the MMAs run
-            c64 cv[kTileNc];
-            const bool live = row < f.m;
+            // the next tile's C entries load while this tile's MMAs finish
+            if (j + 1 < J) {
 #pragma unroll
-            for (int q = 0; q < kTileNc; ++q) {
-                const int col = colbase + q;
-                cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+                for (int q = 0; q < kTileNc; ++q) {
+                    const int col = colbase + kTileNc + q;
+                    nv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+                }
             }
             const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
             if (!__all_sync(0xffffffffu, got)) {
@@ -326,7 +387,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 break;
             }
             tc_fence_after();
-            const uint32_t base = tmem + (uint32_t)(sidx * kTmemCols) + ((uint32_t)(warp * 32) << 16);
+            const uint32_t base = lane_base + kTmemAcc + (uint32_t)(sidx * kTmemCols);
 #pragma unroll
             for (int c0 = 0; c0 < 2 * kTileNc; c0 += 16) {
                 uint32_t r[16];
@@ -338,6 +399,9 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                     cv[c0 / 2 + q].y -= __uint_as_float(r[2 * q + 1]);
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bar_epi[sidx]);
             if (live) {
 #pragma unroll
                 for (int q = 0; q < kTileNc; ++q) {
@@ -345,14 +409,13 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                     if (col < f.m) F[row + (int64_t)col * ld] = cv[q];
                 }
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&bar_epi[sidx]);
+#pragma unroll
+            for (int q = 0; q < kTileNc; ++q) cv[q] = nv[q];
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) tmem_dealloc(tmem, 2 * kTmemCols);
+    if (warp == 4) tmem_dealloc(tmem, kTmemAlloc);
 }
 
 }  // namespace tc
@@ -363,7 +426,6 @@ int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, in
     const int rts = (max_trail + kTileM - 1) / kTileM;
     const int cts = (max_trail + kTileNc - 1) / kTileNc;
     if (rts < 1 || cts < 1) return FDFD_OK;
-    tc::k_pack_a<<<dim3(nfl, rts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
     tc::k_pack_b<<<dim3(nfl, cts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
     const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
     tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, scratch,
