@@ -70,6 +70,22 @@ struct FrontD {
     } while (0)
 
 // ---------------------------------------------------------------------------
+// Operator coefficients [5][n] (centre, then the four neighbour directions)
+// evaluated once per factorization.  stencil_row evaluates the coefficient
+// formulas in FP64, whose rate on this GPU is a small fraction of FP32, so
+// the assembly of the fronts and every refinement residual read the stored
+// values instead of re-deriving them per cell (and per neighbour for A^T).
+__global__ void k_coef(OpDev o, double2 *coef) {
+    const int64_t n = (int64_t)o.Nx * o.Ny;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        double2 c[5];
+        stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
+#pragma unroll
+        for (int d = 0; d < 5; ++d) coef[d * n + k] = c[d];
+    }
+}
+
 // max |A[k,k]| over the grid, as the bit pattern of a non-negative double.
 __global__ void k_maxdiag(OpDev o, unsigned long long *out) {
     const int64_t n = (int64_t)o.Nx * o.Ny;
@@ -586,37 +602,45 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
 // ---- substitutions of levels whose fronts have at most 64 pivots --------------
 // One CTA per front does the whole step of a direction (the gather, the
 // triangular product with the stored inverse and the update rows), instead
-// of a gather launch plus one launch per panel.  Rows of the column-major
-// front go to consecutive lanes, so every product streams the front down
-// its columns; the four thread groups split a sum by column and meet in
-// shared memory.
+// of a gather launch plus one launch per panel.  Products are taken 32 rows
+// at a time: the rows go to consecutive lanes, so each load instruction
+// reads 32 consecutive entries of a column of the column-major front, and
+// eight thread groups split every sum by column (eight loads in flight per
+// row) before meeting in shared memory.
 constexpr int kSmallThreads = 256;
 constexpr int kSmallMaxM = 2048;  // fronts up to this size use the one-launch steps
 constexpr size_t kSmallSmemMax = 200 * 1024;
+constexpr int kSmallGroups = kSmallThreads / 32;
 
 template <typename T>
 __host__ __device__ __forceinline__ size_t small_smem_bytes(int nrhs, int maxm) {
-    return ((size_t)nrhs * maxm + 4 * 64) * sizeof(T);
+    return ((size_t)(nrhs + 1) * maxm + kSmallThreads) * sizeof(T);
 }
 
-// sum over t in [t_lo, t_hi) of F[row, t] v[t], the range split over the four
-// groups (t = g mod 4); returns the total in group 0 (row < 64).
-template <typename T>
-__device__ __forceinline__ T split_rowdot(const T *F, int64_t ld, int row, bool live, int t_lo, int t_hi,
-                                          const T *v, T *part) {
-    const int g = threadIdx.x >> 6, rr = threadIdx.x & 63;
-    T s = czero<T>();
-    if (live)
-        for (int t = t_lo + g; t < t_hi; t += 4) cmac(s, F[row + (int64_t)t * ld], v[t]);
-    part[g * 64 + rr] = s;
-    __syncthreads();
-    T tot = czero<T>();
-    if (g == 0) {
+// res[i] = sum_t F[row0 + i, t] v[t] for i < nrows, with t in [lo, hi)
+// (RANGE = 0), t < row0 + i (RANGE = 1) or t in [row0 + i, hi) (RANGE = 2).
+template <typename T, int RANGE>
+__device__ __forceinline__ void rows_dot(const T *F, int64_t ld, int row0, int nrows, int lo, int hi, const T *v,
+                                         T *part, T *res) {
+    const int rr = threadIdx.x & 31, g = threadIdx.x >> 5;
+    for (int c = 0; c < nrows; c += 32) {
+        const int i = c + rr, row = row0 + i;
+        T s = czero<T>();
+        if (i < nrows) {
+            const int a = (RANGE == 2) ? row : (RANGE == 1 ? 0 : lo);
+            const int e = (RANGE == 1) ? row : hi;
+            for (int t = a + g; t < e; t += kSmallGroups) cmac(s, F[row + (int64_t)t * ld], v[t]);
+        }
+        part[g * 32 + rr] = s;
+        __syncthreads();
+        if (g == 0 && i < nrows) {
+            T tot = part[rr];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) tot = cadd(tot, part[q * 64 + rr]);
+            for (int q = 1; q < kSmallGroups; ++q) tot = cadd(tot, part[q * 32 + rr]);
+            res[i] = tot;
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    return tot;
 }
 
 template <typename T>
@@ -625,8 +649,9 @@ __global__ void __launch_bounds__(kSmallThreads)
                 const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
                 int nrhs, int f_begin, int maxm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *ws = reinterpret_cast<T *>(smem_raw);  // [rhs][maxm]
-    T *part = ws + (size_t)nrhs * maxm;        // [4][64]
+    T *ws = reinterpret_cast<T *>(smem_raw);   // [rhs][maxm]
+    T *tmp = ws + (size_t)nrhs * maxm;          // [maxm]
+    T *part = tmp + maxm;                       // [groups][32]
     const FrontD f = fr[f_begin + blockIdx.x];
     const int32_t *v = vars + f.voff;
     const int tid = threadIdx.x;
@@ -648,28 +673,21 @@ __global__ void __launch_bounds__(kSmallThreads)
     }
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
-    const int rr = tid & 63;
-    // y = inv(L11) w_P (unit diagonal): y_r = w_r + sum_{t<r} invL[r][t] w_t
     for (int r = 0; r < nrhs; ++r) {
         T *w = ws + r * maxm;
-        const T s = split_rowdot(F, ld, rr, rr < f.p, 0, rr, w, part);
-        T y = czero<T>();
-        if (tid < f.p) {
-            y = cadd(w[tid], s);
-            Y[r * sum_m + f.voff + tid] = y;
+        // y = inv(L11) w_P (unit diagonal): y_i = w_i + sum_{t<i} invL[i][t] w_t
+        rows_dot<T, 1>(F, ld, 0, f.p, 0, 0, w, part, tmp);
+        for (int i = tid; i < f.p; i += blockDim.x) {
+            const T y = cadd(w[i], tmp[i]);
+            w[i] = y;
+            Y[r * sum_m + f.voff + i] = y;
         }
-        __syncthreads();  // every thread has read w[0:p]
-        if (tid < f.p) w[tid] = y;
         __syncthreads();
-    }
-    // w_B -= L21 y, one thread per update row
-    for (int r = 0; r < nrhs; ++r) {
-        const T *y = ws + r * maxm;
-        for (int row = f.p + tid; row < f.m; row += blockDim.x) {
-            T s = y[row];
-            for (int t = 0; t < f.p; ++t) cmsub(s, F[row + (int64_t)t * ld], y[t]);
-            W[r * sum_m + f.voff + row] = s;
-        }
+        // update rows: w_B -= L21 y
+        rows_dot<T, 0>(F, ld, f.p, f.m - f.p, 0, f.p, w, part, tmp);
+        for (int i = tid; i < f.m - f.p; i += blockDim.x)
+            W[r * sum_m + f.voff + f.p + i] = csub(w[f.p + i], tmp[i]);
+        __syncthreads();
     }
 }
 
@@ -679,7 +697,8 @@ __global__ void __launch_bounds__(kSmallThreads)
                 const T *__restrict__ Y, double2 *x, int64_t sum_m, int64_t n, int nrhs, int f_begin, int maxm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // [rhs][maxm]: pivots then x_B
-    T *part = xs + (size_t)nrhs * maxm;
+    T *tmp = xs + (size_t)nrhs * maxm;
+    T *part = tmp + maxm;
     const FrontD f = fr[f_begin + blockIdx.x];
     const int32_t *v = vars + f.voff;
     const int tid = threadIdx.x;
@@ -688,16 +707,16 @@ __global__ void __launch_bounds__(kSmallThreads)
     __syncthreads();
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
-    const int rr = tid & 63;
     for (int r = 0; r < nrhs; ++r) {
         T *xr = xs + r * maxm;
         // acc = y - U12 x_B
-        const T s = split_rowdot(F, ld, rr, rr < f.p, f.p, f.m, xr, part);
-        if (tid < f.p) xr[tid] = csub(Y[r * sum_m + f.voff + tid], s);
+        rows_dot<T, 0>(F, ld, 0, f.p, f.p, f.m, xr, part, tmp);
+        for (int i = tid; i < f.p; i += blockDim.x) xr[i] = csub(Y[r * sum_m + f.voff + i], tmp[i]);
         __syncthreads();
-        // x_P = inv(U11) acc: x_r = sum_{t>=r} invU[r][t] acc_t
-        const T xv = split_rowdot(F, ld, rr, rr < f.p, rr, f.p, xr, part);
-        if (tid < f.p) x[r * n + v[tid]] = to_c128(xv, 1.0);
+        // x_P = inv(U11) acc: x_i = sum_{t>=i} invU[i][t] acc_t
+        rows_dot<T, 2>(F, ld, 0, f.p, 0, f.p, xr, part, tmp);
+        for (int i = tid; i < f.p; i += blockDim.x) x[r * n + v[i]] = to_c128(tmp[i], 1.0);
+        __syncthreads();
     }
 }
 
@@ -1135,6 +1154,11 @@ struct fdfd_factor {
     void *d_bwd_scratch = nullptr;
     double pivot_tol = -1.0;  // relative static-pivot threshold (<0: default)
     int fused_max_m = -1;     // largest front factored in one launch (<0: shared-memory limit)
+    // coefficients of the factored operator (see k_coef) and the operator
+    // description they belong to
+    double2 *d_coef = nullptr;
+    fdfd_operator coef_op{};
+    bool coef_valid = false;
     // tensor-core Schur path (FDFD_PREC_C64_TC)
     bool use_tc = false;
     std::vector<char> tc_level;
@@ -1775,7 +1799,7 @@ void free_factor(fdfd_factor *f) {
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
                     f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
                     f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch, f->d_krylov,
-                    f->d_units, f->d_flags};
+                    f->d_units, f->d_flags, f->d_coef};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -1918,6 +1942,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += (int64_t)S.nf * sizeof(FrontD);
     b += 2 * S.sum_m * 4 + 6 * n * 4;                    // vars, relmap, nbr, var maps
     b += (int64_t)(S.Nx + S.Ny) * 16;
+    b += 5 * n * 16;                                     // operator coefficients
     b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
     if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
     b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
@@ -2014,7 +2039,8 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
               alloc((void **)&f->d_partial, norms_partial_count(max_nrhs) * 8) &&
               alloc((void **)&f->d_norm, max_nrhs * 8) && alloc((void **)&f->d_sin, max_nrhs * 8) &&
               alloc((void **)&f->d_sout, max_nrhs * 8) && alloc((void **)&f->d_unit, 8 * 8) &&
-              alloc((void **)&f->d_maxdiag, 8) && alloc((void **)&f->d_tiny, 4);
+              alloc((void **)&f->d_maxdiag, 8) && alloc((void **)&f->d_tiny, 4) &&
+              alloc((void **)&f->d_coef, 5 * n * 16);
     if (!ok) {
         free_factor(f);
         return fail(FDFD_ERR_OOM, "factor_create: device allocation failed");
@@ -2116,6 +2142,19 @@ extern "C" int fdfd_factor_set_fused_limit(fdfd_factor *fac, int32_t max_m) {
     return FDFD_OK;
 }
 
+// The refinement residual of an operator that is the factored one (same
+// description: grid, scalars and device buffers) reads the coefficients
+// stored at fdfd_factor_numeric.
+static bool same_operator(const fdfd_operator &a, const fdfd_operator &b) {
+    return a.Nx == b.Nx && a.Ny == b.Ny && a.pol == b.pol && a.averaging == b.averaging && a.omega == b.omega &&
+           a.L0 == b.L0 && a.xlen == b.xlen && a.ylen == b.ylen && a.eps == b.eps && a.eps_add == b.eps_add &&
+           a.diag_add == b.diag_add && a.inv_sxf == b.inv_sxf && a.inv_sxb == b.inv_sxb &&
+           a.inv_syf == b.inv_syf && a.inv_syb == b.inv_syb && a.stencil == b.stencil;
+}
+static void use_stored_coefficients(const fdfd_factor *fac, const fdfd_operator *op, OpDev *o) {
+    if (fac->coef_valid && !o->stencil && same_operator(*op, fac->coef_op)) o->stencil = fac->d_coef;
+}
+
 extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, void *stream) {
     if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_numeric: NULL factor");
     OpDev o;
@@ -2130,10 +2169,19 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
         CUDA_TRY(cudaMemcpyAsync(fac->d_isyf, op->inv_syf, fac->Ny * 16, cudaMemcpyDeviceToDevice, st));
     }
     CUDA_TRY(cudaEventRecord(fac->ev[0], st));
+    fac->coef_valid = false;
+    if (!o.stencil) {
+        prof_begin(PROF_ASSEMBLE, st);
+        k_coef<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_coef);
+        prof_end(PROF_ASSEMBLE, st, 1);
+        o.stencil = fac->d_coef;
+    }
     rc = (fac->precision != FDFD_PREC_C128) ? factor_levels<c64, float>(fac, o, st)
                                             : factor_levels<c128, double>(fac, o, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[1], st));
+    fac->coef_op = *op;
+    fac->coef_valid = !op->stencil;
     fac->numeric_done = true;
     return FDFD_OK;
 }
@@ -2164,6 +2212,7 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
     if (rc) return rc;
     if (op->Nx != fac->Nx || op->Ny != fac->Ny)
         return fail(FDFD_ERR_BAD_ARG, "solve_refined: operator grid differs from the factor grid");
+    use_stored_coefficients(fac, op, &o);
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n = fac->n;
     const double2 *bb = (const double2 *)b;
@@ -2235,6 +2284,7 @@ extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const
     if (rc) return rc;
     if (op->Nx != fac->Nx || op->Ny != fac->Ny)
         return fail(FDFD_ERR_BAD_ARG, "solve_gmres: operator grid differs from the factor grid");
+    use_stored_coefficients(fac, op, &o);
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n = fac->n;
     const int m = restart;

@@ -226,7 +226,7 @@ __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__
 // Every wait is bounded; on time-out a thread records an error, the
 // producer waits (bounded) for the copies it issued, and the CTA frees its
 // tensor memory and returns.
-constexpr int kColTilesPerCta = 8;
+constexpr int kColTilesPerCta = 16;
 constexpr int kStages = 3;
 constexpr uint32_t kStageBytes = 2 * kBTileBytes;
 constexpr uint32_t kSmemBytes = kStages * kStageBytes + 256;

@@ -229,10 +229,15 @@ int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op,
  * x = A^-T b (transpose = 1), complex128 in and out, nrhs columns.       */
 int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x,
                       int32_t nrhs, int32_t transpose, void *stream);
-/* Solve with FP64 iterative refinement against the matrix-free operator
- * until max_j ||b_j - A x_j|| / ||b_j|| <= tol or max_iter steps.
- * Replaces solver_direct (fdfdpy/linalg.py:122-149).  Returns
- * FDFD_ERR_NOT_CONVERGED (x still written) when tol was not reached.    */
+/* Solve with FP64 iterative refinement against the operator `op` until
+ * max_j ||b_j - A x_j|| / ||b_j|| <= tol or max_iter steps.  When `op`
+ * describes the factored operator (same grid, scalars and device buffers
+ * as at fdfd_factor_numeric) the residual reads the operator coefficients
+ * stored by fdfd_factor_numeric (operator buffers changed in place since
+ * then need a new fdfd_factor_numeric); any other operator is applied
+ * matrix-free.  Replaces solver_direct (fdfdpy/linalg.py:122-149).
+ * Returns FDFD_ERR_NOT_CONVERGED (x still written) when tol was not
+ * reached.                                                               */
 int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
                        const void *b, void *x, int32_t nrhs,
                        int32_t transpose, double tol, int32_t max_iter,

@@ -213,3 +213,22 @@ def test_cooperative_levels_solve(eng, prec, nrhs):
     x = fac.solve(b, tol=1e-11, max_iter=30, raise_on_fail=True).cpu().numpy().reshape(nrhs, -1)
     for k in range(nrhs):
         assert np.linalg.norm(A @ x[k] - b[k]) / np.linalg.norm(b[k]) < 1e-11
+
+
+def test_refinement_against_another_operator(eng):
+    """The factor of one operator preconditions the refinement for a nearby
+    operator: the residual is taken with the operator passed to the solve
+    (applied matrix-free), not the stored coefficients of the factored one."""
+    Nx, Ny = 90, 80
+    eps, A, rng = _problem(Nx, Ny, "Hz", seed=41)
+    eps2 = eps * 1.002
+    A2 = O.construct_A(OMEGA, Nx * 0.02, Ny * 0.02, eps2, [6, 5], "Hz", 1e-6)
+    op1 = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Hz", 1e-6)
+    op2 = eng.DeviceOperator(OMEGA, eps2, Nx * 0.02, Ny * 0.02, [6, 5], "Hz", 1e-6)
+    fac = eng.Factor(eng.Symbolic(Nx, Ny), "c128").numeric(op1)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    x1 = fac.solve(b, tol=1e-12, max_iter=5, raise_on_fail=True).cpu().numpy()
+    assert np.linalg.norm(A @ x1 - b) / np.linalg.norm(b) < 1e-12
+    x2 = fac.solve(b, tol=1e-12, max_iter=60, op=op2, raise_on_fail=True).cpu().numpy()
+    assert np.linalg.norm(A2 @ x2 - b) / np.linalg.norm(b) < 1e-12
+    assert fac.stats()["refine_iters"] > 1
