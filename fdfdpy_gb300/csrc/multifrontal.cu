@@ -1159,6 +1159,9 @@ struct fdfd_factor {
     double2 *d_coef = nullptr;
     fdfd_operator coef_op{};
     bool coef_valid = false;
+    // look-ahead stream of the tensor-core factorization and its fork/join events
+    cudaStream_t st_look = nullptr;
+    cudaEvent_t ev_look[2] = {nullptr, nullptr};
     // tensor-core Schur path (FDFD_PREC_C64_TC)
     bool use_tc = false;
     std::vector<char> tc_level;
@@ -1178,12 +1181,60 @@ namespace {
 
 
 // A level is factored front-by-front in one launch when all its fronts have
-// at most 64 pivots and the largest front fits in shared memory.
+// at most 64 pivots and the largest front fits in shared memory (and under
+// the caller's size limit, if set).
 template <typename T>
 bool dense_front_fits(const fdfd_factor *fac, int maxp, int maxm) {
     if (maxp > kDenseMaxPiv || maxm <= 0) return false;
     if (fac->fused_max_m >= 0 && maxm > fac->fused_max_m) return false;
     return dense_lu_smem<T>(maxm) <= kDenseSmemMax;
+}
+
+// Tensor-core levels with several panels: the diagonal block of panel k+1
+// is factored on a second stream while the Schur update of panel k runs.
+// Per panel: both triangular updates, the U-panel pack, the update of the
+// next panel's 64 columns, then (fork) the next diagonal block on the
+// look-ahead stream beside the update of the remaining columns (join
+// before the next triangular updates, which need both).
+template <typename T, typename R>
+int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp, R tiny, cudaStream_t st) {
+    T *pool = (T *)fac->d_pool;
+    cudaStream_t s2 = fac->st_look;
+    constexpr int kNextTiles = NB / kTileNc;  // column tiles of the next panel
+    prof_begin(PROF_LU_DIAG, st);
+    k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), st>>>(fac->d_fronts, pool, fb, 0, 0, tiny,
+                                                                        fac->d_tiny);
+    prof_end(PROF_LU_DIAG, st, 1);
+    for (int k0 = 0; k0 < maxp; k0 += NB) {
+        const int trail = maxm - k0 - 1;  // upper bound of m - t0
+        if (trail <= 0) continue;
+        const int tiles = (trail + BM - 1) / BM;
+        prof_begin(PROF_TRSM, st);
+        k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+        prof_end(PROF_TRSM, st, 1);
+        prof_begin(PROF_SCHUR, st);
+        int rc = tc_pack_b(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, fac->d_scratch, st);
+        if (rc) return rc;
+        const bool next = k0 + NB < maxp;
+        if (next) {
+            rc = tc_schur_cols(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, 0, kNextTiles, fac->d_scratch,
+                               fac->d_tcerr, st);
+            if (rc) return rc;
+            CUDA_TRY(cudaEventRecord(fac->ev_look[0], st));
+            CUDA_TRY(cudaStreamWaitEvent(s2, fac->ev_look[0], 0));
+            prof_begin(PROF_LU_DIAG, s2);
+            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), s2>>>(fac->d_fronts, pool, fb, k0 + NB, 0,
+                                                                                tiny, fac->d_tiny);
+            prof_end(PROF_LU_DIAG, s2, 1);
+            CUDA_TRY(cudaEventRecord(fac->ev_look[1], s2));
+        }
+        rc = tc_schur_cols(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, next ? kNextTiles : 0, 1 << 30,
+                           fac->d_scratch, fac->d_tcerr, st);
+        if (rc) return rc;
+        prof_end(PROF_SCHUR, st, next ? 3 : 2);
+        if (next) CUDA_TRY(cudaStreamWaitEvent(st, fac->ev_look[1], 0));
+    }
+    return FDFD_OK;
 }
 
 template <typename T, typename R>
@@ -1232,6 +1283,12 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             prof_end(PROF_LU_DIAG, st, 1);
             continue;
         }
+        const bool tc = std::is_same<T, c64>::value && fac->use_tc && fac->tc_level[L];
+        if (tc && maxp > NB && fac->st_look) {
+            int rc = factor_level_lookahead<T, R>(fac, fb, nfl, maxm, maxp, tiny, st);
+            if (rc) return rc;
+            continue;
+        }
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
             k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), st>>>(fac->d_fronts, pool, fb, k0, 0,
@@ -1244,7 +1301,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
             prof_end(PROF_TRSM, st, 1);
             prof_begin(PROF_SCHUR, st);
-            if (std::is_same<T, c64>::value && fac->use_tc && fac->tc_level[L]) {
+            if (tc) {
                 int rc = tc_schur_step(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch,
                                        fac->d_tcerr, st);
                 if (rc) return rc;
@@ -1806,6 +1863,9 @@ void free_factor(fdfd_factor *f) {
     if (f->h_err) cudaFreeHost(f->h_err);
     for (auto &e : f->ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : f->ev_look)
+        if (e) cudaEventDestroy(e);
+    if (f->st_look) cudaStreamDestroy(f->st_look);
     delete f;
 }
 
@@ -2074,6 +2134,14 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         if (e == cudaSuccess) e = cudaMemset(f->d_tcerr, 0, 4);
         if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
         if (rc == FDFD_OK) rc = tc_prepare();
+        if (rc == FDFD_OK) {
+            int lo = 0, hi = 0;
+            e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&f->st_look, cudaStreamNonBlocking, hi);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_look[0], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_look[1], cudaEventDisableTiming);
+            if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+        }
     }
     if (rc == FDFD_OK) {
         std::vector<int64_t> coff;

@@ -30,6 +30,7 @@
 // its tensor memory and returns.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "cplx.cuh"
@@ -240,16 +241,16 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 __global__ void __launch_bounds__(kCtaThreads, 1)
-    k_schur_tc(const TcFront *__restrict__ fr, c64 *pool, int f_begin, int k0, const uint8_t *scratch,
-               int *err) {
+    k_schur_tc(const TcFront *__restrict__ fr, c64 *pool, int f_begin, int k0, int ct_lo, int ct_hi,
+               const uint8_t *scratch, int *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const TcFront f = fr[f_begin + blockIdx.x];
     const int w = min(kPanel, f.p - k0);
     if (w <= 0) return;
     const int t0 = k0 + w, mt = f.m - t0;
     const int rt = blockIdx.y;
-    const int cts = (mt + kTileNc - 1) / kTileNc;
-    const int ct0 = blockIdx.z * kColTilesPerCta;
+    const int cts = min((mt + kTileNc - 1) / kTileNc, ct_hi);
+    const int ct0 = ct_lo + blockIdx.z * kColTilesPerCta;
     if (rt * kTileM >= mt || ct0 >= cts) return;
     const int J = min(kColTilesPerCta, cts - ct0);
 
@@ -421,15 +422,39 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
 }  // namespace tc
 
 // ---- host launchers ------------------------------------------------------------
+int tc_pack_b(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, uint8_t *scratch,
+              cudaStream_t st) {
+    const int cts = (max_trail + kTileNc - 1) / kTileNc;
+    if (cts < 1) return FDFD_OK;
+    tc::k_pack_b<<<dim3(nfl, cts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("pack_b: ") + cudaGetErrorString(e));
+    return FDFD_OK;
+}
+
+int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, int ct_lo,
+                  int ct_hi, const uint8_t *scratch, int *err, cudaStream_t st) {
+    const int rts = (max_trail + kTileM - 1) / kTileM;
+    const int cts = std::min((max_trail + kTileNc - 1) / kTileNc, ct_hi) - ct_lo;
+    if (rts < 1 || cts < 1) return FDFD_OK;
+    const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
+    tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, ct_lo,
+                                                                                ct_hi, scratch, err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("schur_tc: ") + cudaGetErrorString(e));
+    return FDFD_OK;
+}
+
 int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail,
                   uint8_t *scratch, int *err, cudaStream_t st) {
+    int rc = tc_pack_b(fr, pool, f_begin, nfl, k0, max_trail, scratch, st);
+    if (rc) return rc;
     const int rts = (max_trail + kTileM - 1) / kTileM;
     const int cts = (max_trail + kTileNc - 1) / kTileNc;
     if (rts < 1 || cts < 1) return FDFD_OK;
-    tc::k_pack_b<<<dim3(nfl, cts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
     const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
-    tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, scratch,
-                                                                                err);
+    tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, 0, cts,
+                                                                                scratch, err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("schur_tc: ") + cudaGetErrorString(e));
     return FDFD_OK;

@@ -31,6 +31,12 @@ inline int64_t tc_front_scratch(int m, int p, int64_t *a_bytes) {
 
 int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail,
                   uint8_t *scratch, int *err, cudaStream_t st);
+// The two halves of a step, for a look-ahead schedule: pack the U panel,
+// then update the column tiles [ct_lo, ct_hi) of the trailing block.
+int tc_pack_b(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, uint8_t *scratch,
+              cudaStream_t st);
+int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, int ct_lo,
+                  int ct_hi, const uint8_t *scratch, int *err, cudaStream_t st);
 int tc_prepare();
 
 }  // namespace fdfd

@@ -167,7 +167,7 @@ def test_whole_front_and_panel_kernels_agree(eng, prec, leaf):
     b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
     xr = O.solve(A, b)
     xs = []
-    for limit in (-1, 0):
+    for limit in (-1, 0, 100000):  # default, never, as large as shared memory allows
         fac = eng.Factor(sym, prec, fused_max_m=limit).numeric(op)
         x0 = fac.apply_inverse(b).cpu().numpy()  # one application, no refinement
         if prec == "c128":
@@ -177,7 +177,8 @@ def test_whole_front_and_panel_kernels_agree(eng, prec, leaf):
         x = fac.solve(b, tol=1e-12 if prec == "c128" else 1e-10, max_iter=40, raise_on_fail=True)
         xs.append(x.cpu().numpy())
         assert rel(xs[-1], xr) < (1e-10 if prec == "c128" else 1e-8), limit
-    assert rel(xs[0], xs[1]) < (1e-10 if prec == "c128" else 1e-8)
+    for x in xs[1:]:
+        assert rel(xs[0], x) < (1e-10 if prec == "c128" else 1e-8)
 
 
 def test_static_pivot_lifts_are_counted_on_both_paths(eng):
