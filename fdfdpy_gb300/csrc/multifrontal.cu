@@ -140,30 +140,31 @@ __global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
     }
 }
 
-// Extend-add: the parent pulls child `slot`'s update matrix.
+// Extend-add: the parent pulls child `slot`'s update matrix.  A CTA takes
+// `cb` consecutive columns of the child's update block and spreads all of
+// their entries over its threads (rows fastest), so a small update block
+// (28 x 28 at the leaves) still keeps every thread busy and every thread
+// has several independent load-add-store chains.
 template <typename T>
 __global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__restrict__ relmap,
-                             T *pool, int f_begin, int slot) {
+                             T *pool, int f_begin, int slot, int cb) {
     const FrontD f = fr[f_begin + blockIdx.x];
     const int c = slot ? f.c1 : f.c0;
     if (c < 0) return;
     const FrontD ch = fr[c];
     const int mu = ch.m - ch.p;
-    constexpr int CB = 8;
-    const int b0 = blockIdx.y * CB;
+    const int b0 = blockIdx.y * cb;
     if (b0 >= mu) return;
     const int32_t *rm = relmap + ch.voff + ch.p;
     const T *U = pool + ch.f_off + (int64_t)ch.p * ch.ld + ch.p;
     T *P = pool + f.f_off;
     const int64_t ldc = ch.ld, ldp = f.ld;
-    const int bend = min(b0 + CB, mu);
-    for (int b = b0; b < bend; ++b) {
-        const int64_t pc = (int64_t)rm[b] * ldp;
-        for (int a = threadIdx.x; a < mu; a += blockDim.x) {
-            const T u = U[a + b * ldc];
-            T &dst = P[rm[a] + pc];
-            dst = cadd(dst, u);
-        }
+    const int cols = min(cb, mu - b0);
+    const int total = cols * mu;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+        const int bb = idx / mu, a = idx - bb * mu, b = b0 + bb;
+        T &dst = P[rm[a] + (int64_t)rm[b] * ldp];
+        dst = cadd(dst, U[a + (int64_t)b * ldc]);
     }
 }
 
@@ -1267,10 +1268,12 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
                     if (c >= 0) maxmu = std::max(maxmu, S.m[c] - S.p[c]);
             }
             if (maxmu > 0) {
-                dim3 g(nfl, (maxmu + 7) / 8);
+                // about 2048 entries per CTA; at most (1 << 30) / maxmu columns so idx fits in int
+                const int cb = std::max(1, 2048 / maxmu);
+                dim3 g(nfl, (maxmu + cb - 1) / cb);
                 prof_begin(PROF_EXTEND_ADD, st);
-                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 0);
-                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 1);
+                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 0, cb);
+                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 1, cb);
                 prof_end(PROF_EXTEND_ADD, st, 2);
             }
         }
