@@ -95,18 +95,37 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def schur_flops(sym, nb=64):
-    """Algorithmic real flops of the Schur-complement GEMMs of one factor:
-    sum over fronts and panels of 8 w (m - k0 - w)^2."""
+def schur_work(sym, elem=8, nb=64):
+    """Algorithmic work of the Schur-complement updates of one factor run by
+    the Schur kernels (levels not factored whole in shared memory): real
+    flops 8 w t^2 and bytes (C read and written once, L and U panels read
+    once) elem * (2 t^2 + 2 t w) per front and panel, t = m - k0 - w."""
     info = sym.info
     p = sym.export(0, info.n_fronts).astype(np.int64)
     m = sym.export(1, info.n_fronts).astype(np.int64)
-    tot = 0.0
+    lp = sym.export(7, info.n_levels + 1).astype(np.int64)
+    keep = np.ones(info.n_fronts, dtype=bool)
+    for L in range(info.n_levels):
+        sl = slice(lp[L], lp[L + 1])
+        S = (int(m[sl].max()) + 15) // 16 * 16
+        if int(p[sl].max()) <= nb and S * (S + 1) * elem <= 220 * 1024:  # whole-front kernel
+            keep[sl] = False
+    p, m = p[keep], m[keep]
+    flops = byts = 0.0
     for k0 in range(0, int(p.max()), nb):
         w = np.clip(p - k0, 0, nb)
         t = np.where(w > 0, m - k0 - w, 0)
-        tot += float(np.sum(8.0 * w * t * t))
-    return tot
+        flops += float(np.sum(8.0 * w * t * t))
+        byts += float(np.sum(elem * (2.0 * t * t + 2.0 * t * w)))
+    return flops, byts
+
+
+# DRAM bytes measured by ncu on one k_schur_tc launch of this workload (the
+# main update of the first panel step of level 16: a 6077 x 6013 complex
+# block; read 314.11 MB + write 231.68 MB against 590.85 MB algorithmic)
+# divided by that launch's algorithmic bytes; used to report the traffic
+# of an average launch.
+TC_TRAFFIC_RATIO = 545.79 / 590.85
 
 
 def run_ours(args, rank, world):
@@ -372,15 +391,15 @@ def main():
     value = world * 1e3 / ms
     prof = res["profile"]
     schur_ms, schur_n = prof["schur"]
-    fl = schur_flops(res["sym"])
-    achieved = fl / (schur_ms * 1e-3) / 1e12 if schur_ms > 0 else None
+    fl, by = schur_work(res["sym"], 16 if args.precision == "c128" else 8)
+    achieved = by / (schur_ms * 1e-3) / 1e9 if schur_ms > 0 else None
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peaks = json.load(f)
-        peak, peak_src = float(peaks["bf16_tflops"]), "measured"
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
     except Exception:
-        peak, peak_src = 1900.0, "fallback"
+        peak, peak_src = 6800.0, "fallback"
     cpu = None
     if os.environ.get("FDFD_BENCH_NO_CPU") != "1":
         dt, ext, _ = cpu_baseline_sample(args.cpu_sample)
@@ -403,12 +422,17 @@ def main():
         "mixed": {"rel_residual": res["stats64"]["rel_residual"], "refine_iters": res["stats64"]["refine_iters"],
                   "tiny_pivots": res["stats64"]["tiny_pivots"],
                   "field_err_vs_c128": res.get("field_err_vs_c128")},
-        "roofline": {"kernel": ("k_schur_tc (tcgen05 kind::tf32, 3xTF32 complex Schur update) on fronts with "
-                               "m >= 512, k_gemm<c64,SCHUR> (SIMT) below" if args.precision == "c64tc"
-                               else "k_gemm<c64,SCHUR> (SIMT complex FP32 Schur update)"), "bound": "tensor",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "peak_source": f"{peak_src} dense bf16", "algorithmic_flops_per_step": fl,
+        "roofline": {"kernel": ("Schur-complement update: k_schur_tc (tcgen05 kind::tf32, 3xTF32) on fronts "
+                               "with m >= 512, k_schur_simt below" if args.precision == "c64tc"
+                               else "Schur-complement update: k_schur_simt (SIMT complex)"),
+                     "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": (TC_TRAFFIC_RATIO * by / schur_n) if (TC_TRAFFIC_RATIO and schur_n
+                                                                      and args.precision == "c64tc") else None,
+                     "peak_source": f"{peak_src} HBM copy bandwidth",
+                     "algorithmic_bytes_per_step": by, "algorithmic_flops_per_step": fl,
+                     "useful_tflops": fl / (schur_ms * 1e-3) / 1e12 if schur_ms > 0 else None,
                      "launches_per_step": schur_n, "ms_per_step": schur_ms},
         "kernel_classes_ms": {k: round(v[0], 3) for k, v in prof.items()},
         "cpu_baseline": cpu,

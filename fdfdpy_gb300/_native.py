@@ -97,14 +97,15 @@ SIGNATURES = {
     "fdfd_profile_read": (C.c_int, [I32, P, P]),
 }
 
-PROFILE_CLASSES = ("assemble", "extend_add", "lu_diag", "trsm", "schur", "solve_fwd", "solve_bwd", "other")
+PROFILE_CLASSES = ("assemble", "extend_add", "lu_diag", "trsm", "schur", "solve_fwd", "solve_bwd", "other", "pack")
 
 
 def profile_read():
     """{class: (ms, launches)} accumulated since the last reset."""
-    ms = (C.c_double * 8)()
-    cnt = (C.c_int64 * 8)()
-    call("fdfd_profile_read", 8, ms, cnt)
+    nc = len(PROFILE_CLASSES)
+    ms = (C.c_double * nc)()
+    cnt = (C.c_int64 * nc)()
+    call("fdfd_profile_read", nc, ms, cnt)
     return {k: (ms[i], cnt[i]) for i, k in enumerate(PROFILE_CLASSES)}
 
 _lib = None

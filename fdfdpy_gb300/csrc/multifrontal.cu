@@ -281,8 +281,10 @@ __device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_
             if (i < kw && j < kw) B[i + j * LD] = (i > j) ? li[i][j] : ui[i][j];
 }
 
+// complex64: at most 80 registers so that three CTAs share an SM (the
+// leaves' fronts are latency-bound; 2 CTAs per SM ran 1.7x slower there).
 template <typename T, typename R>
-__global__ void __launch_bounds__(kDenseThreads) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
+__global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
                                                             int k0, int whole, R tiny, int *tiny_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *D = reinterpret_cast<T *>(smem_raw);
@@ -1213,9 +1215,11 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
         prof_begin(PROF_TRSM, st);
         k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
         prof_end(PROF_TRSM, st, 1);
-        prof_begin(PROF_SCHUR, st);
+        prof_begin(PROF_PACK, st);
         int rc = tc_pack_b(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, fac->d_scratch, st);
         if (rc) return rc;
+        prof_end(PROF_PACK, st, 1);
+        prof_begin(PROF_SCHUR, st);
         const bool next = k0 + NB < maxp;
         if (next) {
             rc = tc_schur_cols(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, 0, kNextTiles, fac->d_scratch,
@@ -1232,7 +1236,7 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
         rc = tc_schur_cols(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, next ? kNextTiles : 0, 1 << 30,
                            fac->d_scratch, fac->d_tcerr, st);
         if (rc) return rc;
-        prof_end(PROF_SCHUR, st, next ? 3 : 2);
+        prof_end(PROF_SCHUR, st, next ? 2 : 1);
         if (next) CUDA_TRY(cudaStreamWaitEvent(st, fac->ev_look[1], 0));
     }
     return FDFD_OK;
@@ -1303,13 +1307,18 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             prof_begin(PROF_TRSM, st);
             k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
             prof_end(PROF_TRSM, st, 1);
-            prof_begin(PROF_SCHUR, st);
             if (tc) {
-                int rc = tc_schur_step(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch,
-                                       fac->d_tcerr, st);
+                prof_begin(PROF_PACK, st);
+                int rc = tc_pack_b(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch, st);
                 if (rc) return rc;
-                prof_end(PROF_SCHUR, st, 2);
+                prof_end(PROF_PACK, st, 1);
+                prof_begin(PROF_SCHUR, st);
+                rc = tc_schur_cols(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, 0, 1 << 30, fac->d_scratch,
+                                   fac->d_tcerr, st);
+                if (rc) return rc;
+                prof_end(PROF_SCHUR, st, 1);
             } else {
+                prof_begin(PROF_SCHUR, st);
                 k_schur_simt<T, R><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
                 prof_end(PROF_SCHUR, st, 1);
             }

@@ -445,21 +445,6 @@ int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, in
     return FDFD_OK;
 }
 
-int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail,
-                  uint8_t *scratch, int *err, cudaStream_t st) {
-    int rc = tc_pack_b(fr, pool, f_begin, nfl, k0, max_trail, scratch, st);
-    if (rc) return rc;
-    const int rts = (max_trail + kTileM - 1) / kTileM;
-    const int cts = (max_trail + kTileNc - 1) / kTileNc;
-    if (rts < 1 || cts < 1) return FDFD_OK;
-    const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
-    tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, 0, cts,
-                                                                                scratch, err);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("schur_tc: ") + cudaGetErrorString(e));
-    return FDFD_OK;
-}
-
 int tc_prepare() {
     cudaError_t e = cudaFuncSetAttribute(tc::k_schur_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tc::kSmemBytes);

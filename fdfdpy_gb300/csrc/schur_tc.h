@@ -29,10 +29,9 @@ inline int64_t tc_front_scratch(int m, int p, int64_t *a_bytes) {
     return cts * 2 * (int64_t)kBTileBytes;
 }
 
-int tc_schur_step(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail,
-                  uint8_t *scratch, int *err, cudaStream_t st);
-// The two halves of a step, for a look-ahead schedule: pack the U panel,
-// then update the column tiles [ct_lo, ct_hi) of the trailing block.
+// One panel step in two calls: pack the U panel (hi/lo TF32 B'' tiles),
+// then update the column tiles [ct_lo, ct_hi) of the trailing block (the
+// look-ahead schedule splits the update in two column ranges).
 int tc_pack_b(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, uint8_t *scratch,
               cudaStream_t st);
 int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, int ct_lo,
