@@ -723,6 +723,132 @@ __global__ void __launch_bounds__(kSmallThreads)
     }
 }
 
+// Levels of small fronts (m <= 128): one warp per front, eight fronts per
+// CTA.  A lane owns rows (lane, lane + 32, ...) of the front and streams
+// the column-major entries of its rows column by column (32 consecutive
+// entries per load instruction, several columns in flight), with the
+// vectors in the warp's shared memory; no block barrier is involved.
+constexpr int kWarpMaxM = 128;
+constexpr int kWarpFronts = 8;
+
+template <typename T>
+__host__ __device__ __forceinline__ size_t warp_smem_bytes(int nrhs, int maxm) {
+    return (size_t)kWarpFronts * nrhs * maxm * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpFronts)
+    k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+               const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
+               int nrhs, int f_begin, int nfl, int maxm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int fi = blockIdx.x * kWarpFronts + warp;
+    if (fi >= nfl) return;
+    T *ws = reinterpret_cast<T *>(smem_raw) + (size_t)warp * nrhs * maxm;
+    const FrontD f = fr[f_begin + fi];
+    const int32_t *v = vars + f.voff;
+    const int p = f.p, m = f.m;
+    for (int r = 0; r < nrhs; ++r)
+        for (int k = lane; k < m; k += 32) ws[r * maxm + k] = (k < p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+    __syncwarp();
+    for (int slot = 0; slot < 2; ++slot) {
+        const int c = slot ? f.c1 : f.c0;
+        if (c < 0) continue;
+        const FrontD ch = fr[c];
+        const int mu = ch.m - ch.p;
+        const int32_t *rm = relmap + ch.voff + ch.p;
+        for (int r = 0; r < nrhs; ++r) {
+            const T *wc = W + r * sum_m + ch.voff + ch.p;
+            for (int a = lane; a < mu; a += 32) ws[r * maxm + rm[a]] = cadd(ws[r * maxm + rm[a]], wc[a]);
+        }
+        __syncwarp();
+    }
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int r0 = lane, r1 = lane + 32;
+    for (int r = 0; r < nrhs; ++r) {
+        T *w = ws + r * maxm;
+        // y = inv(L11) w_P: y_i = w_i + sum_{t<i} invL[i][t] w_t (rows r0, r1 < p <= 64)
+        T a0 = czero<T>(), a1 = czero<T>();
+#pragma unroll 8
+        for (int t = 0; t < p; ++t) {
+            const T wt = w[t];
+            if (t < r0) cmac(a0, F[r0 + (int64_t)t * ld], wt);
+            if (t < r1 && r1 < p) cmac(a1, F[r1 + (int64_t)t * ld], wt);
+        }
+        __syncwarp();
+        if (r0 < p) {
+            const T y = cadd(w[r0], a0);
+            w[r0] = y;
+            Y[r * sum_m + f.voff + r0] = y;
+        }
+        if (r1 < p) {
+            const T y = cadd(w[r1], a1);
+            w[r1] = y;
+            Y[r * sum_m + f.voff + r1] = y;
+        }
+        __syncwarp();
+        // update rows: w_B -= L21 y
+        for (int rb = p; rb < m; rb += 32) {
+            const int row = rb + lane;
+            T a = czero<T>();
+            if (row < m) {
+#pragma unroll 8
+                for (int t = 0; t < p; ++t) cmac(a, F[row + (int64_t)t * ld], w[t]);
+                W[r * sum_m + f.voff + row] = csub(w[row], a);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpFronts)
+    k_bwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const T *__restrict__ pool,
+               const T *__restrict__ Y, double2 *x, int64_t sum_m, int64_t n, int nrhs, int f_begin, int nfl,
+               int maxm) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int fi = blockIdx.x * kWarpFronts + warp;
+    if (fi >= nfl) return;
+    T *xs = reinterpret_cast<T *>(smem_raw) + (size_t)warp * nrhs * maxm;
+    const FrontD f = fr[f_begin + fi];
+    const int32_t *v = vars + f.voff;
+    const int p = f.p, m = f.m;
+    for (int r = 0; r < nrhs; ++r)
+        for (int k = p + lane; k < m; k += 32) xs[r * maxm + k] = from_c128<T>(x[r * n + v[k]], 1.0);
+    __syncwarp();
+    const T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    const int r0 = lane, r1 = lane + 32;
+    for (int r = 0; r < nrhs; ++r) {
+        T *xr = xs + r * maxm;
+        // acc = y - U12 x_B
+        T a0 = czero<T>(), a1 = czero<T>();
+#pragma unroll 8
+        for (int c = p; c < m; ++c) {
+            const T xc = xr[c];
+            if (r0 < p) cmac(a0, F[r0 + (int64_t)c * ld], xc);
+            if (r1 < p) cmac(a1, F[r1 + (int64_t)c * ld], xc);
+        }
+        if (r0 < p) xr[r0] = csub(Y[r * sum_m + f.voff + r0], a0);
+        if (r1 < p) xr[r1] = csub(Y[r * sum_m + f.voff + r1], a1);
+        __syncwarp();
+        // x_P = inv(U11) acc: x_i = sum_{t>=i} invU[i][t] acc_t
+        T s0 = czero<T>(), s1 = czero<T>();
+#pragma unroll 8
+        for (int t = 0; t < p; ++t) {
+            const T at = xr[t];
+            if (t >= r0) cmac(s0, F[r0 + (int64_t)t * ld], at);
+            if (t >= r1 && r1 < p) cmac(s1, F[r1 + (int64_t)t * ld], at);
+        }
+        if (r0 < p) x[r * n + v[r0]] = to_c128(s0, 1.0);
+        if (r1 < p) x[r * n + v[r1]] = to_c128(s1, 1.0);
+        __syncwarp();
+    }
+}
+
 // ---- shared panel-step helpers of the triangular solves ------------------------
 // Shared memory of one panel step: the w x w diagonal block (only its
 // triangle), the input vector block and the result block, staged with
@@ -1673,6 +1799,8 @@ int set_smem_attrs() {
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
     return FDFD_OK;
 }
@@ -1681,6 +1809,10 @@ int set_smem_attrs() {
 // s_in / s_out are device arrays of per-column scales.
 // Levels whose fronts all have at most 64 pivots take the one-launch steps
 // of each direction when their vectors fit in shared memory.
+template <typename T>
+bool warp_level_fits(int maxp, int maxm, int nrhs) {
+    return maxp <= NB && maxm <= kWarpMaxM && warp_smem_bytes<T>(nrhs, maxm) <= kSmallSmemMax;
+}
 template <typename T>
 bool small_level_fits(int maxp, int maxm, int nrhs) {
     return maxp <= NB && maxm <= kSmallMaxM && small_smem_bytes<T>(nrhs, maxm) <= kSmallSmemMax;
@@ -1726,6 +1858,13 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             continue;
         }
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
+        if (warp_level_fits<T>(maxp, maxm, nrhs)) {
+            k_fwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
+                            st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, nfl,
+                                  maxm);
+            prof_end(PROF_SOLVE_FWD, st, 1);
+            continue;
+        }
         if (small_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_small<T><<<nfl, kSmallThreads, small_smem_bytes<T>(nrhs, maxm), st>>>(
                 fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, maxm);
@@ -1768,6 +1907,13 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             const int grid = std::max(1, std::min(fac->coop_grid, items));
             CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
+            prof_end(PROF_SOLVE_BWD, st, 1);
+            continue;
+        }
+        if (warp_level_fits<T>(maxp, S.lev_max_m[L], nrhs)) {
+            const int maxm = S.lev_max_m[L];
+            k_bwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
+                            st>>>(fac->d_fronts, fac->d_vars, pool, Y, x, sum_m, n, nrhs, fb, nfl, maxm);
             prof_end(PROF_SOLVE_BWD, st, 1);
             continue;
         }
