@@ -1562,12 +1562,24 @@ __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool
                                             const unsigned *flags, unsigned epoch, int *err, T *vs,
                                             T (&acc)[8]) {
     const int rr = threadIdx.x >> 2, t0 = 16 * (threadIdx.x & 3);
-    for (int k = k_first; k != k_last; k += k_step) {
-        const int c0 = k * NB, w = min(NB, p - c0);
-        T a[16];
+    // the tile of the next panel is loaded while this panel waits and computes
+    T a[16], an[16];
+    if (k_first != k_last) {
+        const int w = min(NB, p - k_first * NB);
 #pragma unroll
         for (int i = 0; i < 16; ++i)
-            a[i] = (live && t0 + i < w) ? F[(r0 + rr) + (int64_t)(c0 + t0 + i) * ld] : czero<T>();
+            an[i] = (live && t0 + i < w) ? F[(r0 + rr) + (int64_t)(k_first * NB + t0 + i) * ld] : czero<T>();
+    }
+    for (int k = k_first; k != k_last; k += k_step) {
+        const int c0 = k * NB, w = min(NB, p - c0);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) a[i] = an[i];
+        if (k + k_step != k_last) {
+            const int cn = (k + k_step) * NB, wn = min(NB, p - cn);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+                an[i] = (live && t0 + i < wn) ? F[(r0 + rr) + (int64_t)(cn + t0 + i) * ld] : czero<T>();
+        }
         if (!wait_flag(flags + k, epoch, err)) return false;
         for (int idx = threadIdx.x; idx < nrhs * NB; idx += blockDim.x) {
             const int r = idx / NB, i = idx % NB;
@@ -1619,7 +1631,7 @@ __device__ __forceinline__ T diag_rows(const T *Ds, const T *vr, int rn, int row
 }
 
 template <typename T, typename R>
-__global__ void __launch_bounds__(kRowsPerCta)
+__global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
@@ -1699,7 +1711,7 @@ __global__ void __launch_bounds__(kRowsPerCta)
 }
 
 template <typename T, typename R>
-__global__ void __launch_bounds__(kRowsPerCta)
+__global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
                 T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
@@ -2186,7 +2198,7 @@ int coop_grid_for(int max_nrhs, int *grid) {
     const size_t smem = std::max(panel_smem_bytes<T>(max_nrhs), (size_t)max_nrhs * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_fwd_level<T, R>, kRowsPerCta, smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_bwd_level<T, R>, kRowsPerCta, smem));
-    const int per_sm = std::min(std::min(nb1, nb2), 2);
+    const int per_sm = std::min(std::min(nb1, nb2), 4);
     *grid = per_sm > 0 ? per_sm * sms : 0;
     return FDFD_OK;
 }

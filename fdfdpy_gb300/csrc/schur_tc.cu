@@ -146,11 +146,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 __device__ __forceinline__ void tmem_ld_wait() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ float to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
 
 // Shared-memory matrix descriptor, no swizzle, K-major canonical layout:
 // core matrices of 8 rows x 16 bytes; lbo = byte distance between the two
@@ -169,12 +164,6 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 }
 
 // ---- packing ---------------------------------------------------------------
-// Byte offset of real element (row r in [0,rows), k in [0,128)) inside a
-// packed K-major tile with `groups` 8-row groups.
-__device__ __forceinline__ uint32_t pack_off(int r, int k, int groups) {
-    const int s = k >> 3, ki = (k >> 2) & 1, e = k & 3, mi = r >> 3, rr = r & 7;
-    return (uint32_t)(s * (2 * groups * 128) + ki * (groups * 128) + mi * 128 + rr * 16 + e * 4);
-}
 
 // B'' tiles: grid (front, column tile), 256 threads.
 __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__ pool, int f_begin, int k0,
@@ -188,25 +177,12 @@ __global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__
     uint8_t *hi = scratch + f.b_off + (size_t)ct * 2 * kBTileBytes;
     uint8_t *lo = hi + kBTileBytes;
     const c64 *F = pool + f.f_off;
-    constexpr int G = 2 * kTileNc / 8;
     for (int idx = threadIdx.x; idx < kTileNc * kPanel; idx += blockDim.x) {
         const int l = idx % kPanel, j = idx / kPanel;
         const int col = t0 + ct * kTileNc + j;
         c64 v = czero<c64>();
         if (col < f.m && l < w) v = F[(k0 + l) + (int64_t)col * f.ld];
-        const float re_h = to_tf32(v.x), im_h = to_tf32(v.y);
-        const float re_l = to_tf32(v.x - re_h), im_l = to_tf32(v.y - im_h);
-        // (2l, 2j) = re, (2l+1, 2j) = -im, (2l, 2j+1) = im, (2l+1, 2j+1) = re;
-        // B'' is stored N-row major over K: row n' = 2j + c, column k' = 2l + a.
-        const int n0 = 2 * j, n1 = 2 * j + 1, ka = 2 * l, kb = 2 * l + 1;
-        *(float *)(hi + pack_off(n0, ka, G)) = re_h;
-        *(float *)(hi + pack_off(n0, kb, G)) = -im_h;
-        *(float *)(hi + pack_off(n1, ka, G)) = im_h;
-        *(float *)(hi + pack_off(n1, kb, G)) = re_h;
-        *(float *)(lo + pack_off(n0, ka, G)) = re_l;
-        *(float *)(lo + pack_off(n0, kb, G)) = -im_l;
-        *(float *)(lo + pack_off(n1, ka, G)) = im_l;
-        *(float *)(lo + pack_off(n1, kb, G)) = re_l;
+        tc_store_b(hi, lo, l, j, v);
     }
 }
 
@@ -350,11 +326,11 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 const int l = 16 * c + q;
                 c64 v = czero<c64>();
                 if (live && l < w) v = F[row + (int64_t)(k0 + l) * ld];
-                const float hx = to_tf32(v.x), hy = to_tf32(v.y);
+                const float hx = tc_to_tf32(v.x), hy = tc_to_tf32(v.y);
                 hi[2 * q] = __float_as_uint(hx);
                 hi[2 * q + 1] = __float_as_uint(hy);
-                lo[2 * q] = __float_as_uint(to_tf32(v.x - hx));
-                lo[2 * q + 1] = __float_as_uint(to_tf32(v.y - hy));
+                lo[2 * q] = __float_as_uint(tc_to_tf32(v.x - hx));
+                lo[2 * q + 1] = __float_as_uint(tc_to_tf32(v.y - hy));
             }
             tmem_st32(lane_base + kTmemAHi + 32 * c, hi);
             tmem_st32(lane_base + kTmemALo + 32 * c, lo);
