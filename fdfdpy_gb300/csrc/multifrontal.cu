@@ -454,7 +454,7 @@ enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
 // (TRSM_U) of its output and reads all of them before writing.
 template <typename T, typename R, int MODE>
 __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, int ytile,
-                                          int ztile, T (*As)[BM + 1], T (*Bs)[BN + 1]) {
+                                          int ztile, T (*As)[BM + 1], T (*Bs)[BN + 1], uint8_t *bpack = nullptr) {
     const FrontD f = fr[f_begin + blockIdx.x];
     const int w = min(NB, f.p - k0);
     if (w <= 0) return;
@@ -546,6 +546,25 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
             else dst = acc[qa][qb];
         }
     }
+    if constexpr (MODE == TRSM_U && std::is_same<T, c64>::value) {
+        // tensor-core levels: the U panel also goes straight into its packed
+        // B'' tiles (hi/lo TF32), zero outside the panel and the front
+        if (bpack) {
+            const int cts = (m - t0 + kTileNc - 1) / kTileNc;
+#pragma unroll
+            for (int qa = 0; qa < 4; ++qa) {
+                const int r = rbase + ty + 16 * qa, l = r - k0;
+#pragma unroll
+                for (int qb = 0; qb < 4; ++qb) {
+                    const int c = cbase + tx + 16 * qb, cc = c - t0, ct = cc / kTileNc;
+                    if (ct >= cts) continue;
+                    const c64 v = (r < rend && c < cend) ? acc[qa][qb] : czero<c64>();
+                    uint8_t *hi = bpack + (size_t)ct * 2 * kBTileBytes;
+                    tc_store_b(hi, hi + kBTileBytes, l, cc - ct * kTileNc, v);
+                }
+            }
+        }
+    }
 }
 
 template <typename T, typename R>
@@ -557,15 +576,18 @@ __global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ f
 
 // Both triangular updates of a panel step in one launch: blockIdx.z = 0
 // forms L (row tile blockIdx.y), blockIdx.z = 1 forms U (column tile
-// blockIdx.y).
+// blockIdx.y) and, on tensor-core levels (tcf != NULL), its packed tiles.
 template <typename T, typename R>
-__global__ void __launch_bounds__(256) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0) {
+__global__ void __launch_bounds__(256) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
+                                                    const TcFront *__restrict__ tcf, uint8_t *scratch) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
-    if (blockIdx.z == 0)
+    if (blockIdx.z == 0) {
         gemm_tile<T, R, TRSM_L>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
-    else
-        gemm_tile<T, R, TRSM_U>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs);
+    } else {
+        uint8_t *bpack = tcf ? scratch + tcf[f_begin + blockIdx.x].b_off : nullptr;
+        gemm_tile<T, R, TRSM_U>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
+    }
 }
 
 // ---- solve ------------------------------------------------------------------
@@ -1339,13 +1361,11 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
         if (trail <= 0) continue;
         const int tiles = (trail + BM - 1) / BM;
         prof_begin(PROF_TRSM, st);
-        k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+        k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0, fac->d_tcf,
+                                                                fac->d_scratch);
         prof_end(PROF_TRSM, st, 1);
-        prof_begin(PROF_PACK, st);
-        int rc = tc_pack_b(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, fac->d_scratch, st);
-        if (rc) return rc;
-        prof_end(PROF_PACK, st, 1);
         prof_begin(PROF_SCHUR, st);
+        int rc = FDFD_OK;
         const bool next = k0 + NB < maxp;
         if (next) {
             rc = tc_schur_cols(fac->d_tcf, (c64 *)pool, fb, nfl, k0, trail, 0, kNextTiles, fac->d_scratch,
@@ -1431,15 +1451,13 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             if (trail <= 0) continue;
             const int tiles = (trail + BM - 1) / BM;
             prof_begin(PROF_TRSM, st);
-            k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
+            k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0,
+                                                                    tc ? fac->d_tcf : nullptr,
+                                                                    tc ? fac->d_scratch : nullptr);
             prof_end(PROF_TRSM, st, 1);
             if (tc) {
-                prof_begin(PROF_PACK, st);
-                int rc = tc_pack_b(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, fac->d_scratch, st);
-                if (rc) return rc;
-                prof_end(PROF_PACK, st, 1);
                 prof_begin(PROF_SCHUR, st);
-                rc = tc_schur_cols(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, 0, 1 << 30, fac->d_scratch,
+                int rc = tc_schur_cols(fac->d_tcf, (c64 *)fac->d_pool, fb, nfl, k0, trail, 0, 1 << 30, fac->d_scratch,
                                    fac->d_tcerr, st);
                 if (rc) return rc;
                 prof_end(PROF_SCHUR, st, 1);

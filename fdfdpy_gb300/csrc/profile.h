@@ -16,8 +16,7 @@ enum ProfClass {
     PROF_SOLVE_FWD = 5,
     PROF_SOLVE_BWD = 6,
     PROF_OTHER = 7,
-    PROF_PACK = 8,
-    PROF_NCLASS = 9
+    PROF_NCLASS = 8
 };
 
 void prof_begin(int cls, cudaStream_t st);

@@ -163,40 +163,19 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
     return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// ---- packing ---------------------------------------------------------------
-
-// B'' tiles: grid (front, column tile), 256 threads.
-__global__ void k_pack_b(const TcFront *__restrict__ fr, const c64 *__restrict__ pool, int f_begin, int k0,
-                         uint8_t *scratch) {
-    const TcFront f = fr[f_begin + blockIdx.x];
-    const int w = min(kPanel, f.p - k0);
-    if (w <= 0) return;
-    const int t0 = k0 + w, mt = f.m - t0;
-    const int ct = blockIdx.y;
-    if (ct * kTileNc >= mt) return;
-    uint8_t *hi = scratch + f.b_off + (size_t)ct * 2 * kBTileBytes;
-    uint8_t *lo = hi + kBTileBytes;
-    const c64 *F = pool + f.f_off;
-    for (int idx = threadIdx.x; idx < kTileNc * kPanel; idx += blockDim.x) {
-        const int l = idx % kPanel, j = idx / kPanel;
-        const int col = t0 + ct * kTileNc + j;
-        c64 v = czero<c64>();
-        if (col < f.m && l < w) v = F[(k0 + l) + (int64_t)col * f.ld];
-        tc_store_b(hi, lo, l, j, v);
-    }
-}
-
 // ---- the GEMM ------------------------------------------------------------------
 // One CTA = one 128-row tile of C and up to kColTilesPerCta 32-column tiles,
 // warp-specialized:
-//   warps 0-3 first write the tile's A' rows (hi and lo TF32 parts of the L
-//     panel, read straight from the front) into tensor memory -- thread =
-//     TMEM lane = row -- so the MMAs read A from TMEM and only B from shared
-//     memory; then they drain the accumulators (tcgen05.ld of their 32 TMEM
-//     lanes, C -= acc), the next tile's C entries already loading;
-//   warp 5 (lane 0) streams the B'' tiles (hi, lo) through kStages shared-
+//   warps 0-7 (two per TMEM lane quarter, each with half of the columns)
+//     first write the tile's A' rows (hi and lo TF32 parts of the L panel,
+//     read straight from the front) into tensor memory -- thread = TMEM
+//     lane = row -- so the MMAs read A from TMEM and only B from shared
+//     memory; then they drain the accumulators (tcgen05.ld, C -= acc), the
+//     next tile's C entries already loading (eight warps keep twice the C
+//     loads in flight of four);
+//   warp 9 (lane 0) streams the B'' tiles (hi, lo) through kStages shared-
 //     memory stages, refilling a stage once the MMAs that read it are done;
-//   warp 4 (lane 0) issues the 48 MMAs of each column tile (16 K-steps x 3)
+//   warp 8 (lane 0) issues the 48 MMAs of each column tile (16 K-steps x 3)
 //     into one of two TMEM accumulators and commits them to the epilogue's
 //     barrier and to the stage's release barrier.
 // TMEM columns: A hi [0,128), A lo [128,256), accumulators [256,384).
@@ -208,7 +187,9 @@ constexpr int kStages = 3;
 constexpr uint32_t kStageBytes = 2 * kBTileBytes;
 constexpr uint32_t kSmemBytes = kStages * kStageBytes + 256;
 constexpr uint32_t kWaitLimit = 1u << 22;
-constexpr int kCtaThreads = 192;
+constexpr int kEpiWarps = 8;       // two per TMEM lane quarter, each half of a tile's columns
+constexpr int kMmaWarp = kEpiWarps, kLoadWarp = kEpiWarps + 1;
+constexpr int kCtaThreads = 32 * (kEpiWarps + 2);
 constexpr uint32_t kTmemAlloc = 512;
 constexpr uint32_t kTmemAHi = 0, kTmemALo = 2 * kPanel, kTmemAcc = 4 * kPanel;
 
@@ -238,18 +219,18 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        mbar_init(bar_a, 4);
+        mbar_init(bar_a, kEpiWarps);
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&bar_full[s], 1);
             mbar_init(&bar_free[s], 1);
         }
         mbar_init(&bar_mma[0], 1);
         mbar_init(&bar_mma[1], 1);
-        mbar_init(&bar_epi[0], 4);
-        mbar_init(&bar_epi[1], 4);
+        mbar_init(&bar_epi[0], kEpiWarps);
+        mbar_init(&bar_epi[1], kEpiWarps);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 4) {
+    if (warp == kMmaWarp) {
         tmem_alloc(tmem_slot, kTmemAlloc);
         tmem_relinquish();
     }
@@ -258,7 +239,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 5) {
+    if (warp == kLoadWarp) {
         if (lane == 0) {
             bool ok = true;
             int issued = 0;
@@ -280,7 +261,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 mbar_wait_bounded(&bar_full[j % kStages], (j / kStages) & 1, kWaitLimit);
             if (!ok) atomicExch(err, 3);
         }
-    } else if (warp == 4) {
+    } else if (warp == kMmaWarp) {
         if (lane == 0) {
             bool ok = mbar_wait_bounded(bar_a, 0, kWaitLimit);
             constexpr uint32_t idesc = idesc_tf32(kTileM, 2 * kTileNc);
@@ -311,15 +292,19 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
             if (!ok) atomicExch(err, 1);
         }
     } else {
-        // warps 0-3: warp w owns TMEM lanes (tile rows) 32w..32w+31
-        const int row = t0 + rt * kTileM + warp * 32 + lane;
+        // epilogue warp w owns TMEM lanes (tile rows) 32 (w % 4) .. + 31 and
+        // half h = w / 4 of the columns: A' columns [64 h, 64 h + 64), complex
+        // tile columns [16 h, 16 h + 16)
+        const int q4 = warp & 3, h = warp >> 2;
+        constexpr int kHalf = kTileNc / 2;
+        const int row = t0 + rt * kTileM + q4 * 32 + lane;
         const bool live = row < f.m;
         c64 *F = pool + f.f_off;
         const int64_t ld = f.ld;
-        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
         // A' row: (Re, Im) of L[row, k0 + l] at columns (2l, 2l + 1), hi and lo parts
 #pragma unroll 1
-        for (int c = 0; c < 2 * kPanel / 32; ++c) {
+        for (int c = 2 * h; c < 2 * h + 2; ++c) {
             uint32_t hi[32], lo[32];
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
@@ -340,20 +325,20 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(bar_a);
 
-        c64 cv[kTileNc], nv[kTileNc];
+        c64 cv[kHalf], nv[kHalf];
 #pragma unroll
-        for (int q = 0; q < kTileNc; ++q) {
-            const int col = t0 + ct0 * kTileNc + q;
+        for (int q = 0; q < kHalf; ++q) {
+            const int col = t0 + ct0 * kTileNc + kHalf * h + q;
             cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
             nv[q] = czero<c64>();
         }
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
-            const int colbase = t0 + (ct0 + j) * kTileNc;
+            const int colbase = t0 + (ct0 + j) * kTileNc + kHalf * h;
             // the next tile's C entries load while this tile's MMAs finish
             if (j + 1 < J) {
 #pragma unroll
-                for (int q = 0; q < kTileNc; ++q) {
+                for (int q = 0; q < kHalf; ++q) {
                     const int col = colbase + kTileNc + q;
                     nv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
                 }
@@ -364,9 +349,9 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 break;
             }
             tc_fence_after();
-            const uint32_t base = lane_base + kTmemAcc + (uint32_t)(sidx * kTmemCols);
+            const uint32_t base = lane_base + kTmemAcc + (uint32_t)(sidx * kTmemCols + 2 * kHalf * h);
 #pragma unroll
-            for (int c0 = 0; c0 < 2 * kTileNc; c0 += 16) {
+            for (int c0 = 0; c0 < 2 * kHalf; c0 += 16) {
                 uint32_t r[16];
                 tmem_ld16(base + (uint32_t)c0, r);
                 tmem_ld_wait();
@@ -381,33 +366,23 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
             if (lane == 0) mbar_arrive(&bar_epi[sidx]);
             if (live) {
 #pragma unroll
-                for (int q = 0; q < kTileNc; ++q) {
+                for (int q = 0; q < kHalf; ++q) {
                     const int col = colbase + q;
                     if (col < f.m) F[row + (int64_t)col * ld] = cv[q];
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kTileNc; ++q) cv[q] = nv[q];
+            for (int q = 0; q < kHalf; ++q) cv[q] = nv[q];
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 4) tmem_dealloc(tmem, kTmemAlloc);
+    if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemAlloc);
 }
 
 }  // namespace tc
 
 // ---- host launchers ------------------------------------------------------------
-int tc_pack_b(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, uint8_t *scratch,
-              cudaStream_t st) {
-    const int cts = (max_trail + kTileNc - 1) / kTileNc;
-    if (cts < 1) return FDFD_OK;
-    tc::k_pack_b<<<dim3(nfl, cts), 256, 0, st>>>(fr, pool, f_begin, k0, scratch);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("pack_b: ") + cudaGetErrorString(e));
-    return FDFD_OK;
-}
-
 int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, int ct_lo,
                   int ct_hi, const uint8_t *scratch, int *err, cudaStream_t st) {
     const int rts = (max_trail + kTileM - 1) / kTileM;

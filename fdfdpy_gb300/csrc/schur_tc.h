@@ -63,11 +63,9 @@ inline int64_t tc_front_scratch(int m, int p, int64_t *a_bytes) {
     return cts * 2 * (int64_t)kBTileBytes;
 }
 
-// One panel step in two calls: pack the U panel (hi/lo TF32 B'' tiles),
-// then update the column tiles [ct_lo, ct_hi) of the trailing block (the
-// look-ahead schedule splits the update in two column ranges).
-int tc_pack_b(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, uint8_t *scratch,
-              cudaStream_t st);
+// Update of the column tiles [ct_lo, ct_hi) of a panel step's trailing
+// block from the packed B'' tiles of the U panel (written by the panel's
+// triangular update); the look-ahead schedule splits the columns in two.
 int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, int max_trail, int ct_lo,
                   int ct_hi, const uint8_t *scratch, int *err, cudaStream_t st);
 int tc_prepare();
