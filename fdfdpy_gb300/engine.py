@@ -231,6 +231,26 @@ def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
         return s
 
 
+# Device memory of released factors, kept for the next factor of the same
+# grid, precision and right-hand-side count: allocating (and freeing) the
+# ~20 GB of a 2048^2 factor costs tens of milliseconds, a quarter of the
+# solve itself, so a Simulation created per solve reuses it.  Only factors
+# of the process-wide symbolic analyses (symbolic_for, which live as long as
+# the process) are kept, at most one per key; release_cached_factors()
+# frees them.
+_parked = {}
+_parked_lock = threading.Lock()
+
+
+def release_cached_factors():
+    """Frees the device memory of released factors kept for reuse."""
+    with _parked_lock:
+        hs = list(_parked.values())
+        _parked.clear()
+    for h in hs:
+        N.lib().fdfd_factor_destroy(h)
+
+
 class Factor:
     """A numeric multifrontal factorization of one operator on the device."""
 
@@ -239,13 +259,18 @@ class Factor:
             raise ValueError("precision must be 'c128', 'c64' or 'c64tc'")
         device()
         self.sym, self.precision, self.max_nrhs = sym, precision, int(max_nrhs)
-        h = C.c_void_p()
-        N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
+        shared = _sym_cache.get((sym.Nx, sym.Ny, sym.leaf_area)) is sym
+        self._key = (sym.Nx, sym.Ny, sym.leaf_area, precision, self.max_nrhs) if shared else None
+        h = None
+        if self._key is not None:
+            with _parked_lock:
+                h = _parked.pop(self._key, None)
+        if h is None:
+            h = C.c_void_p()
+            N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
         self.handle = h
-        if pivot_tol is not None:
-            N.call("fdfd_factor_set_pivot_tol", h, float(pivot_tol))
-        if fused_max_m is not None:
-            N.call("fdfd_factor_set_fused_limit", h, int(fused_max_m))
+        N.call("fdfd_factor_set_pivot_tol", h, -1.0 if pivot_tol is None else float(pivot_tol))
+        N.call("fdfd_factor_set_fused_limit", h, -1 if fused_max_m is None else int(fused_max_m))
         self.op = None
 
     @staticmethod
@@ -324,9 +349,16 @@ class Factor:
 
     def __del__(self):
         try:
-            if self.handle:
-                N.lib().fdfd_factor_destroy(self.handle)
-                self.handle = None
+            h, self.handle = self.handle, None
+            if h:
+                keep = False
+                if self._key is not None:
+                    with _parked_lock:
+                        keep = self._key not in _parked
+                        if keep:
+                            _parked[self._key] = h
+                if not keep:
+                    N.lib().fdfd_factor_destroy(h)
         except Exception:
             pass
 

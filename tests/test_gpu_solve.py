@@ -233,3 +233,31 @@ def test_refinement_against_another_operator(eng):
     x2 = fac.solve(b, tol=1e-12, max_iter=60, op=op2, raise_on_fail=True).cpu().numpy()
     assert np.linalg.norm(A2 @ x2 - b) / np.linalg.norm(b) < 1e-12
     assert fac.stats()["refine_iters"] > 1
+
+
+def test_released_factor_memory_is_reused(eng):
+    """A factor of the shared symbolic analysis that is released keeps its
+    device memory for the next factor of the same grid and precision; the
+    reused factor is refactored from scratch (a different operator solves
+    to its own solution)."""
+    Nx, Ny = 66, 58
+    eps, A, rng = _problem(Nx, Ny, "Ez", seed=51)
+    eps2 = eps[::-1].copy()
+    A2 = O.construct_A(OMEGA, Nx * 0.02, Ny * 0.02, eps2, [6, 5], "Ez", 1e-6)
+    op1 = eng.DeviceOperator(OMEGA, eps, Nx * 0.02, Ny * 0.02, [6, 5], "Ez", 1e-6)
+    op2 = eng.DeviceOperator(OMEGA, eps2, Nx * 0.02, Ny * 0.02, [6, 5], "Ez", 1e-6)
+    sym = eng.symbolic_for(Nx, Ny)
+    b = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+    f1 = eng.Factor(sym, "c128").numeric(op1)
+    h1 = f1.handle.value
+    assert rel(f1.apply_inverse(b).cpu().numpy(), O.solve(A, b)) < 1e-10
+    del f1
+    f2 = eng.Factor(sym, "c128", pivot_tol=0.3).numeric(op2)
+    assert f2.handle.value == h1
+    assert f2.stats()["tiny_pivots"] > 0  # the new factor's own settings apply
+    f2 = None
+    f3 = eng.Factor(sym, "c128").numeric(op2)
+    assert f3.handle.value == h1 and f3.stats()["tiny_pivots"] == 0
+    assert rel(f3.apply_inverse(b).cpu().numpy(), O.solve(A2, b)) < 1e-10
+    other = eng.Factor(eng.Symbolic(Nx, Ny), "c128")  # a private analysis never takes a parked factor
+    assert other.handle.value != h1
