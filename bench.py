@@ -207,7 +207,7 @@ def run_ours(args, rank, world):
         e2e_step()
     torch.cuda.synchronize()
     res["e2e_s"] = (time.perf_counter() - t0) / ke
-    res["h2d"] = int(eps_h.nbytes + N * N * 16)
+    res["h2d"] = int(eps_h.nbytes + src_h.nbytes)  # eps and the (real) source, float64
     res["d2h"] = int(3 * N * N * 16)
     res["clocks"] = clk.summary()
     res["sym"] = sym

@@ -160,16 +160,21 @@ class Simulation:
             raise ValueError('Invalid polarization: {}'.format(str(self.pol)))
         from time import time
         t = time()
-        b = np.asarray(self.src * 1j * self.omega).astype(np.complex128).reshape((-1,))
         (Nx, Ny) = self.src.shape
-        eps_tot = self.eps_r if not include_nl else self.eps_r + self.eps_nl
-        if not b.any():
+        # b = 1j * omega * src, formed on the device from the uploaded source
+        src = np.asarray(self.src)
+        src_dev = engine.as_f64(src) if not np.iscomplexobj(src) else engine.as_c128(src)
+        b = (src_dev.reshape(-1).to(torch.complex128) * (1j * self.omega)).contiguous()
+        if not bool(torch.any(src_dev != 0)):
             X = torch.zeros(Nx * Ny, dtype=torch.complex128, device=engine.device())
             zero_src = True
         else:
             X = self.solve_device(b, include_nl=include_nl, precision=precision, tol=tol)
             zero_src = False
-        eps_dev = engine.as_f64(eps_tot).reshape(-1) if (include_nl or self.pol == 'Hz') else None
+        if include_nl:
+            eps_dev = engine.as_f64(self.eps_r + self.eps_nl).reshape(-1)
+        else:
+            eps_dev = self._op.eps if self.pol == 'Hz' else None
         f1, f2 = self._op.fields(X, averaging=averaging, eps=eps_dev)
         F1 = f1.cpu().numpy().reshape((Nx, Ny))
         F2 = f2.cpu().numpy().reshape((Nx, Ny))
