@@ -423,7 +423,7 @@ def main():
                   "tiny_pivots": res["stats64"]["tiny_pivots"],
                   "field_err_vs_c128": res.get("field_err_vs_c128")},
         "roofline": {"kernel": ("Schur-complement update: k_schur_tc (tcgen05 kind::tf32, 3xTF32) on fronts "
-                               "with m >= 512, k_schur_simt below" if args.precision == "c64tc"
+                               "with m >= 192, k_schur_simt below" if args.precision == "c64tc"
                                else "Schur-complement update: k_schur_simt (SIMT complex)"),
                      "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

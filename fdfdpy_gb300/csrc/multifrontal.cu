@@ -2058,7 +2058,7 @@ void free_factor(fdfd_factor *f) {
 }
 
 // Tensor-core levels: fronts large enough for 128-row tiles to pay.
-constexpr int kTcMinM = 256;
+constexpr int kTcMinM = 192;
 
 int64_t tc_layout(const Symbolic &S, std::vector<char> *lev, std::vector<TcFront> *tf) {
     int64_t best = 0;
