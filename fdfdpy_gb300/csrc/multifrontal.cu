@@ -518,6 +518,10 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
             }
         }
         __syncthreads();
+        // the triangular inverses are zero below (inv(U), TRSM_L) or above
+        // (inv(L), TRSM_U) their diagonal: K chunk kc adds nothing to the
+        // output columns (rows) of the 16-blocks before it
+        const int kcb = kc / 16;
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
             T a[4], b[4];
@@ -527,9 +531,14 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
                 b[q] = Bs[kk][tx + 16 * q];
             }
 #pragma unroll
-            for (int qa = 0; qa < 4; ++qa)
+            for (int qa = 0; qa < 4; ++qa) {
+                if (MODE == TRSM_U && qa < kcb) continue;
 #pragma unroll
-                for (int qb = 0; qb < 4; ++qb) cmac(acc[qa][qb], a[qa], b[qb]);
+                for (int qb = 0; qb < 4; ++qb) {
+                    if (MODE == TRSM_L && qb < kcb) continue;
+                    cmac(acc[qa][qb], a[qa], b[qb]);
+                }
+            }
         }
         __syncthreads();
     }
