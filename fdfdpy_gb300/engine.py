@@ -237,7 +237,9 @@ def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
 # solve itself, so a Simulation created per solve reuses it.  Only factors
 # of the process-wide symbolic analyses (symbolic_for, which live as long as
 # the process) are kept, at most one per key; release_cached_factors()
-# frees them.
+# frees them.  Work on a factor is asynchronous (and freeing no longer
+# synchronizes the device), so a parked factor carries an event per stream
+# it was used on and its next owner's stream waits for them.
 _parked = {}
 _parked_lock = threading.Lock()
 
@@ -245,7 +247,7 @@ _parked_lock = threading.Lock()
 def release_cached_factors():
     """Frees the device memory of released factors kept for reuse."""
     with _parked_lock:
-        hs = list(_parked.values())
+        hs = [h for h, _ in _parked.values()]
         _parked.clear()
     for h in hs:
         N.lib().fdfd_factor_destroy(h)
@@ -262,9 +264,15 @@ class Factor:
         shared = _sym_cache.get((sym.Nx, sym.Ny, sym.leaf_area)) is sym
         self._key = (sym.Nx, sym.Ny, sym.leaf_area, precision, self.max_nrhs) if shared else None
         h = None
+        self._events = {}
         if self._key is not None:
             with _parked_lock:
-                h = _parked.pop(self._key, None)
+                got = _parked.pop(self._key, None)
+            if got is not None:
+                h, events = got
+                cur = torch.cuda.current_stream()
+                for ev in events:
+                    cur.wait_event(ev)
         if h is None:
             h = C.c_void_p()
             N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
@@ -279,9 +287,17 @@ class Factor:
         N.call("fdfd_factor_bytes", sym.handle, N.PREC[precision], int(max_nrhs), C.byref(b))
         return int(b.value)
 
+    def _used(self):
+        # an event at the end of the work just queued on the current stream
+        st = torch.cuda.current_stream()
+        ev = torch.cuda.Event()
+        ev.record(st)
+        self._events[st.cuda_stream] = ev
+
     def numeric(self, op: DeviceOperator):
         s = op.struct()
         N.call("fdfd_factor_numeric", self.handle, C.byref(s), stream_ptr())
+        self._used()
         self.op = op
         self._op_struct = s
         return self
@@ -303,6 +319,7 @@ class Factor:
             N.call("fdfd_factor_solve", self.handle, _ptr(blk), _ptr(x), blk.shape[0], int(bool(transpose)),
                    stream_ptr())
             outs.append(x)
+        self._used()
         return torch.cat(outs).reshape(b.shape)
 
     def solve(self, b, transpose=False, tol=1e-12, max_iter=10, op: DeviceOperator | None = None,
@@ -330,6 +347,7 @@ class Factor:
             st = self.stats()
             worst, iters = max(worst, st["rel_residual"]), max(iters, st["refine_iters"])
             outs.append(x)
+        self._used()
         self._last = (worst, iters)
         return torch.cat(outs).reshape(b.shape)
 
@@ -356,7 +374,7 @@ class Factor:
                     with _parked_lock:
                         keep = self._key not in _parked
                         if keep:
-                            _parked[self._key] = h
+                            _parked[self._key] = (h, list(self._events.values()))
                 if not keep:
                     N.lib().fdfd_factor_destroy(h)
         except Exception:

@@ -7,9 +7,9 @@ newton_solve: Newton on f(E) = (A + Anl(E)) E - b with the Jacobian
               dAde = dnl_de omega^2 eps0' (nonlinear_solvers.py:57-149).
               The reference solves J11 d + J12 conj(d) = f as a real 2n x 2n
               system with PARDISO (solver_complex2real, linalg.py:152-186);
-              here the complex factor of J11 is the preconditioner of a
-              refinement on that real-linear system (solve_complex2real),
-              so the Newton loop reuses the same GPU multifrontal engine.
+              here the complex factor of J11 preconditions real-inner-product
+              GMRES on that real-linear system (solve_complex2real), so the
+              Newton loop reuses the same GPU multifrontal engine.
 Both keep E on the device between iterations; the Kerr terms are evaluated
 on the device from the Nonlinearity definitions (nonlinearity.py:18-34).
 """
@@ -41,24 +41,76 @@ def kerr_terms_device(simulation, E):
     return eps_nl, dnl_de
 
 
-def solve_complex2real(fac, J11_op, J12, f, tol=1e-12, max_iter=100):
+def solve_complex2real(fac, J11_op, J12, f, tol=1e-12, max_iter=400, restart=60):
     """d with J11 d + J12 * conj(d) = f (J12 a diagonal as an (n,) vector).
 
-    Refinement on the real-linear operator with the factor of J11 as its
-    approximate inverse: d <- d + J11^-1 (f - J11 d - J12 conj(d)); every
-    residual is formed in FP64 with the matrix-free J11.  Returns (d,
-    relative residual, iterations)."""
+    The operator d -> J11 d + J12 conj(d) is linear over the reals (the
+    reference solves it as a real 2n x 2n system, linalg.py:152-186), so
+    this is restarted GMRES in the real inner product Re<u, v> on C^n = R^2n,
+    right-preconditioned by the complex factor of J11: d = J11^-1 y.  A plain
+    fixed-point refinement with that factor diverges once |J12| is
+    comparable to J11 (strong Kerr terms); GMRES does not need the
+    contraction.  Every residual is formed in FP64 with the matrix-free
+    J11.  Returns (d, relative residual, operator applications)."""
     fn = float(torch.linalg.vector_norm(f))
     if fn == 0.0:
         return torch.zeros_like(f), 0.0, 0
-    d = fac.apply_inverse(f)
-    rel, it = float("inf"), 0
-    for it in range(1, max_iter + 1):
-        r = f - J11_op.apply(d) - J12 * torch.conj(d)
-        rel = float(torch.linalg.vector_norm(r)) / fn
-        if rel <= tol:
+
+    def op(x):
+        return J11_op.apply(x) + J12 * torch.conj(x)
+
+    d = torch.zeros_like(f)
+    r = f.clone()
+    beta = fn
+    rel, it = 1.0, 0
+    while it < max_iter:
+        m = min(restart, max_iter - it)
+        V = torch.empty((m + 1,) + tuple(f.shape), dtype=f.dtype, device=f.device)
+        Z = torch.empty((m,) + tuple(f.shape), dtype=f.dtype, device=f.device)
+        V[0] = r / beta
+        H = np.zeros((m + 1, m))
+        cs, sn = np.zeros(m), np.zeros(m)
+        g = np.zeros(m + 1)
+        g[0] = beta
+        k = 0
+        for j in range(m):
+            Z[j] = fac.apply_inverse(V[j])
+            w = op(Z[j])
+            it += 1
+            Vj = V[:j + 1].reshape(j + 1, -1)
+            for _ in range(2):  # classical Gram-Schmidt, twice, real inner product
+                h = torch.real(Vj.conj() @ w.reshape(-1))
+                w = w - (h.to(w.dtype) @ Vj).reshape(w.shape)
+                H[:j + 1, j] += h.cpu().numpy()
+            hn = float(torch.linalg.vector_norm(w))
+            H[j + 1, j] = hn
+            if hn > 0:
+                V[j + 1] = w / hn
+            for i in range(j):  # earlier rotations
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
+                H[i, j] = t
+            den = np.hypot(H[j, j], H[j + 1, j])
+            cs[j], sn[j] = (1.0, 0.0) if den == 0 else (H[j, j] / den, H[j + 1, j] / den)
+            H[j, j] = cs[j] * H[j, j] + sn[j] * H[j + 1, j]
+            H[j + 1, j] = 0.0
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            k = j + 1
+            if abs(g[j + 1]) <= tol * fn or hn == 0:
+                break
+        y = np.linalg.solve(np.triu(H[:k, :k]), g[:k]) if k else np.zeros(0)
+        yt = torch.as_tensor(y, dtype=torch.float64, device=f.device).to(f.dtype)
+        d = d + (yt @ Z[:k].reshape(k, -1)).reshape(f.shape)
+        r = f - op(d)
+        prev, beta = beta, float(torch.linalg.vector_norm(r))
+        rel = beta / fn
+        if rel <= tol or beta == 0.0:
             break
-        d = d + fac.apply_inverse(r)
+        if beta > 0.5 * prev:
+            # a whole cycle gained less than a factor of two on the FP64
+            # residual: it has reached the rounding floor of the operator
+            break
     return d, rel, it
 
 
@@ -114,7 +166,7 @@ def born_solve(simulation, Estart=None, conv_threshold=1e-10, max_num_iter=50, a
 
 
 def newton_solve(simulation, Estart=None, conv_threshold=1e-10, max_num_iter=50, averaging=True,
-                 solver='pardiso', jac_solver='c2r', matrix_format='csr', lin_tol=1e-12):
+                 solver='pardiso', jac_solver='c2r', matrix_format='csr', lin_tol=1e-11):
     conv_array = np.zeros((max_num_iter, 1))
     if simulation.pol != 'Ez':
         raise ValueError('Invalid polarization: {}'.format(str(simulation.pol)))

@@ -50,6 +50,7 @@ class Request:
     cache_hit: bool = False
     rel_residual: float = float("nan")
     refine_iters: int = 0
+    fallback: bool = False        # solved again with a complex128 factor
     error: str | None = None
 
     @property
@@ -126,9 +127,18 @@ class SolveServer:
                 ent = _CacheEntry(op, fac, need, users=1)
                 ent.lock.acquire()
             try:
-                x = fac.solve(torch.from_numpy(req.rhs).to(engine.device(), non_blocking=True),
-                              tol=self.tol, max_iter=self.max_iter, op=op)
+                b = torch.from_numpy(req.rhs).to(engine.device(), non_blocking=True)
+                x = fac.solve(b, tol=self.tol, max_iter=self.max_iter, op=op)
                 st = fac.stats()
+                if not st["rel_residual"] <= self.tol and self.precision != "c128":
+                    # a nearly singular operator (a resonance of this eps) can leave the
+                    # complex64 factor too inaccurate for the refinement to contract:
+                    # solve this request again with a complex128 factor
+                    fac128 = engine.Factor(fac.sym, "c128", max_nrhs=fac.max_nrhs).numeric(op)
+                    x = fac128.solve(b, tol=self.tol, max_iter=self.max_iter, op=op)
+                    st = fac128.stats()
+                    req.fallback = True
+                    del fac128
                 req.x = x.cpu().numpy()
                 req.rel_residual, req.refine_iters = st["rel_residual"], st["refine_iters"]
             except Exception as e:  # reported per request, the server keeps going
@@ -204,6 +214,7 @@ class SolveServer:
             "requests_per_s": len(ok) / makespan if makespan > 0 else float("nan"),
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
             "cache_hits": sum(r.cache_hit for r in ok),
+            "c128_fallbacks": sum(r.fallback for r in ok),
             "max_rel_residual": float(max((r.rel_residual for r in ok), default=float("nan"))),
         }
 
