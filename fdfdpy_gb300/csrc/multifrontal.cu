@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
         // X[B, col] = -inv(L_BB) (L[B, col] + sum), Y[row, B] = -(sum) inv(U_BB)
         T xo[kStep], yo[kStep];
         if (g < b0 && q == 0) {
-            const int col = g, row = g;
+            const int col = g;
 #pragma unroll
             for (int i = 0; i < kStep; ++i)
                 if (i < bs) vl[i] = cadd(vl[i], D[(b0 + i) + col * LD]);
@@ -1303,11 +1303,9 @@ struct fdfd_factor {
     int64_t *d_coop_off = nullptr;
     void *d_coop_scratch = nullptr;
     // pipelined panel units of the cooperative levels (per level: forward
-    // list, backward list) and their completion flags
+    // list, backward list)
     int2 *d_units = nullptr;
-    std::vector<int> unit_fwd_off, unit_fwd_n, unit_bwd_off, unit_bwd_n, lev_kp;
-    unsigned *d_flags = nullptr;
-    unsigned epoch = 0;
+    std::vector<int> unit_fwd_off, unit_fwd_n, unit_bwd_off, unit_bwd_n;
     // two-pass backward opener for levels with wide fronts
     std::vector<char> bwd_wide;
     int64_t *d_bwd_off = nullptr;
@@ -1521,48 +1519,82 @@ __device__ bool grid_sync(GridBar *gb, int *err) {
     return s_ok != 0;
 }
 
-// Completion flags of the pipelined panel units.  A unit publishes its
-// result, then (thread 0, after a fence) stores the launch's epoch into its
-// flag with release semantics; a consumer's thread 0 polls with acquire
-// semantics and the block reads the result through L2 after a barrier.
-// Epochs differ between launches, so flags never need clearing.  The poll is
-// bounded: after kFlagLimit rounds, or once another CTA has reported a
-// failure, the CTA records the error and the block returns.
+// Values passed between the pipelined panel units of one launch carry their
+// own readiness.  Before the launch's grid barrier every slot a unit will
+// publish into is set to kUnset, a signalling-NaN bit pattern that no
+// arithmetic produces (NaN results are quiet), in each 32-bit half of a
+// complex64 slot and each 64-bit half of a complex128 slot.  The producing
+// unit stores the value with relaxed gpu-scope stores; a consumer polls each
+// slot with relaxed gpu-scope loads until no half carries the pattern, so no
+// separate flag, fence or second read is on the chain between units.  The
+// poll is bounded: after kFlagLimit rounds, or once another CTA has reported
+// a failure, the CTA records the error and the block returns.
 constexpr unsigned kFlagLimit = 1u << 22;
+constexpr unsigned kUnset32 = 0x7fa5a5a5u;
+constexpr unsigned long long kUnset64 = 0x7ff4a5a5a5a5a5a5ull;
 
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ void set_unset(c64 *p) {
+    *reinterpret_cast<uint2 *>(p) = make_uint2(kUnset32, kUnset32);
+}
+__device__ __forceinline__ void set_unset(c128 *p) {
+    *reinterpret_cast<ulonglong2 *>(p) = make_ulonglong2(kUnset64, kUnset64);
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const void *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_u64(void *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-__device__ bool wait_flag(const unsigned *flag, unsigned epoch, int *err) {
-    __shared__ int s_go;
-    if (threadIdx.x == 0) {
-        int go = 1;
-        for (unsigned it = 0; ld_acquire_u32(flag) != epoch; ++it) {
-            if (it > kFlagLimit || ((it & 1023u) == 1023u && *(volatile int *)err != 0)) {
-                go = 0;
-                atomicExch(err, 1);
-                break;
+__device__ __forceinline__ void put_value(c64 *p, c64 v) {
+    st_relaxed_u64(p, (unsigned long long)__float_as_uint(v.x) |
+                          ((unsigned long long)__float_as_uint(v.y) << 32));
+}
+__device__ __forceinline__ void put_value(c128 *p, c128 v) {
+    st_relaxed_u64(p, (unsigned long long)__double_as_longlong(v.x));
+    st_relaxed_u64(reinterpret_cast<double *>(p) + 1, (unsigned long long)__double_as_longlong(v.y));
+}
+
+__device__ __forceinline__ bool try_take(const c64 *p, c64 &out) {
+    const unsigned long long v = ld_relaxed_u64(p);
+    const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
+    if (lo == kUnset32 || hi == kUnset32) return false;
+    out = cmake<float>(__uint_as_float(lo), __uint_as_float(hi));
+    return true;
+}
+__device__ __forceinline__ bool try_take(const c128 *p, c128 &out) {
+    const unsigned long long re = ld_relaxed_u64(p);
+    const unsigned long long im = ld_relaxed_u64(reinterpret_cast<const double *>(p) + 1);
+    if (re == kUnset64 || im == kUnset64) return false;
+    out = cmake<double>(__longlong_as_double((long long)re), __longlong_as_double((long long)im));
+    return true;
+}
+
+// Stage one published panel (nrhs x w values at vsrc[r * sum_m + c0 + i])
+// into vs (nrhs x NB, zero past w), waiting for each value.
+template <typename T>
+__device__ bool take_panel(const T *vsrc, int64_t sum_m, int c0, int w, int nrhs, T *vs, int *err) {
+    int fail = 0;
+    for (int idx = threadIdx.x; idx < nrhs * NB && !fail; idx += blockDim.x) {
+        const int r = idx / NB, i = idx % NB;
+        T v = czero<T>();
+        if (i < w) {
+            const T *src = vsrc + r * sum_m + c0 + i;
+            for (unsigned it = 0; !try_take(src, v); ++it) {
+                if (it > kFlagLimit || ((it & 1023u) == 1023u && *(volatile int *)err != 0)) {
+                    fail = 1;
+                    atomicExch(err, 1);
+                    break;
+                }
+                __nanosleep(16);
             }
-            __nanosleep(16);
         }
-        s_go = go;
+        vs[idx] = v;
     }
-    __syncthreads();
-    return s_go != 0;
-}
-
-__device__ __forceinline__ void publish_flag(unsigned *flag, unsigned epoch) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        st_release_u32(flag, epoch);
-    }
+    return __syncthreads_or(fail) == 0;
 }
 
 template <typename T>
@@ -1580,14 +1612,13 @@ __device__ __forceinline__ c128 ldcg_c<c128>(const c128 *p) {
 
 // Pipelined panel unit, the shared part: acc[rhs] (four partial sums per
 // row, rows rr = tid / 4 of the block) -= F[rows, panel] v_panel for each
-// panel in order, where v_panel (a 64-vector per rhs) is read from vsrc
-// (stride sum_m) once the panel's flag carries the epoch.  The panel's
-// matrix tile is loaded before the wait.
+// panel in order, where v_panel (a 64-vector per rhs) is taken from vsrc
+// (stride sum_m) as its values are published.  The panel's matrix tile is
+// loaded before the wait.
 template <typename T>
 __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool live, int k_first, int k_last,
-                                            int k_step, int p, const T *vsrc, int64_t sum_m, int nrhs,
-                                            const unsigned *flags, unsigned epoch, int *err, T *vs,
-                                            T (&acc)[8]) {
+                                            int k_step, int p, const T *vsrc, int64_t sum_m, int nrhs, int *err,
+                                            T *vs, T (&acc)[8]) {
     const int rr = threadIdx.x >> 2, t0 = 16 * (threadIdx.x & 3);
     // the tile of the next panel is loaded while this panel waits and computes
     T a[16], an[16];
@@ -1607,12 +1638,7 @@ __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool
             for (int i = 0; i < 16; ++i)
                 an[i] = (live && t0 + i < wn) ? F[(r0 + rr) + (int64_t)(cn + t0 + i) * ld] : czero<T>();
         }
-        if (!wait_flag(flags + k, epoch, err)) return false;
-        for (int idx = threadIdx.x; idx < nrhs * NB; idx += blockDim.x) {
-            const int r = idx / NB, i = idx % NB;
-            vs[idx] = (i < w) ? ldcg_c(vsrc + r * sum_m + c0 + i) : czero<T>();
-        }
-        __syncthreads();
+        if (!take_panel(vsrc, sum_m, c0, w, nrhs, vs, err)) return false;
         for (int r = 0; r < nrhs; ++r) {
             const T *vr = vs + r * NB + t0;
 #pragma unroll
@@ -1662,18 +1688,20 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
-                int *err, const int2 *__restrict__ units, int nunits, int kpm, unsigned *flags,
-                unsigned epoch) {
+                int *err, const int2 *__restrict__ units, int nunits) {
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    // gather: right-hand side of the pivots and the children's updates
+    // gather: right-hand side of the pivots and the children's updates; the
+    // pivot slots of Y are marked unpublished
     for (int fi = blockIdx.x; fi < nfl; fi += gridDim.x) {
         const FrontD f = fr[fb + fi];
         const int32_t *v = vars + f.voff;
         for (int r = 0; r < nrhs; ++r) {
             T *w = W + r * sum_m + f.voff;
-            for (int k = tid; k < f.m; k += blockDim.x)
+            for (int k = tid; k < f.m; k += blockDim.x) {
                 w[k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+                if (k < f.p) set_unset(Y + r * sum_m + f.voff + k);
+            }
         }
         __syncthreads();
         for (int slot = 0; slot < 2; ++slot) {
@@ -1709,24 +1737,26 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         const int rn = min(NB, (piv ? f.p : f.m) - r0);
         const T *F = pool + f.f_off;
         const int64_t ld = f.ld;
-        if (piv) stage_diag<T, false>(F, ld, r0, rn, Ds);
         const bool live = rr < rn;
+        // the pivot rows of w are final since the gather: load them now, off
+        // the chain between units (each row's q == 0 thread reads back its own)
+        T *wpre = vin + nrhs * NB;
+        if (piv && live && q == 0)
+            for (int r = 0; r < nrhs; ++r) wpre[r * NB + rr] = ldcg_c(W + r * sum_m + f.voff + r0 + rr);
+        if (piv) stage_diag<T, false>(F, ld, r0, rn, Ds);
         T acc[8];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-        if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs,
-                         flags + fi * kpm, epoch, err, vin, acc))
+        if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs, err, vin, acc))
             return;
         quad_reduce(acc, nrhs);
         if (piv) {
             if (live && q == 0)
-                for (int r = 0; r < nrhs; ++r)
-                    vin[r * NB + rr] = csub(ldcg_c(W + r * sum_m + f.voff + r0 + rr), acc[r]);
+                for (int r = 0; r < nrhs; ++r) vin[r * NB + rr] = csub(wpre[r * NB + rr], acc[r]);
             __syncthreads();
             for (int r = 0; r < nrhs; ++r) {
                 const T y = diag_rows<T, false>(Ds, vin + r * NB, rn, rr);
-                if (live && q == 0) Y[r * sum_m + f.voff + r0 + rr] = y;
+                if (live && q == 0) put_value(Y + r * sum_m + f.voff + r0 + rr, y);
             }
-            publish_flag(flags + fi * kpm + rb, epoch);
         } else if (live && q == 0) {
             for (int r = 0; r < nrhs; ++r) {
                 T *d = W + r * sum_m + f.voff + r0 + rr;
@@ -1741,8 +1771,8 @@ template <typename T, typename R>
 __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
-                T *W, const T *__restrict__ Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
-                const int2 *__restrict__ units, int nunits, int kpm, unsigned *flags, unsigned epoch) {
+                T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
+                const int2 *__restrict__ units, int nunits) {
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
@@ -1774,7 +1804,8 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         __syncthreads();
     }
     if (!grid_sync(gb, err)) return;
-    // opener, pass 2: acc = y - sum of the column blocks, in a fixed order
+    // opener, pass 2: acc = y - sum of the column blocks, in a fixed order;
+    // the pivot slots of Y are then marked unpublished (x goes there)
     const int prow2 = (maxp + kRowsPerCta - 1) / kRowsPerCta;
     for (int item = blockIdx.x; item < nfl * prow2; item += gridDim.x) {
         const int fi = item / prow2, rc = item % prow2;
@@ -1787,12 +1818,13 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
                 T acc = Y[r * sum_m + f.voff + row];
                 for (int c = 0; c < nch; ++c) acc = csub(acc, base[((int64_t)c * nrhs + r) * f.p + row]);
                 W[r * sum_m + f.voff + row] = acc;
+                set_unset(Y + r * sum_m + f.voff + row);
             }
         }
     }
     if (!grid_sync(gb, err)) return;
     // pipelined panels, descending: x_R = inv(U_RR) (acc_R - sum_{j>R} U[R, j] x_j),
-    // published in W's pivot rows (and written to the global solution)
+    // published in Y's pivot rows (and written to the global solution)
     T *Ds = xs, *vin = xs + NB * NB;
     const int rr = tid >> 2, q = tid & 3;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
@@ -1803,27 +1835,29 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         const int r0 = rb * NB, rn = min(NB, f.p - r0);
         const T *F = pool + f.f_off;
         const int64_t ld = f.ld;
-        stage_diag<T, true>(F, ld, r0, rn, Ds);
         const bool live = rr < rn;
+        // this unit's rows of acc are final since the opener: load them off
+        // the chain between units
+        T *wpre = vin + nrhs * NB;
+        if (live && q == 0)
+            for (int r = 0; r < nrhs; ++r) wpre[r * NB + rr] = ldcg_c(W + r * sum_m + f.voff + r0 + rr);
+        stage_diag<T, true>(F, ld, r0, rn, Ds);
         T acc[8];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, W + f.voff, sum_m, nrhs, flags + fi * kpm,
-                         epoch, err, vin, acc))
+        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, Y + f.voff, sum_m, nrhs, err, vin, acc))
             return;
         quad_reduce(acc, nrhs);
         if (live && q == 0)
-            for (int r = 0; r < nrhs; ++r)
-                vin[r * NB + rr] = csub(ldcg_c(W + r * sum_m + f.voff + r0 + rr), acc[r]);
+            for (int r = 0; r < nrhs; ++r) vin[r * NB + rr] = csub(wpre[r * NB + rr], acc[r]);
         __syncthreads();
         const int32_t *v = vars + f.voff + r0;
         for (int r = 0; r < nrhs; ++r) {
             const T xv = diag_rows<T, true>(Ds, vin + r * NB, rn, rr);
             if (live && q == 0) {
-                W[r * sum_m + f.voff + r0 + rr] = xv;
+                put_value(Y + r * sum_m + f.voff + r0 + rr, xv);
                 x[r * n + v[rr]] = to_c128(xv, 1.0);
             }
         }
-        publish_flag(flags + fi * kpm + rb, epoch);
         __syncthreads();
     }
 }
@@ -1857,12 +1891,6 @@ bool small_level_fits(int maxp, int maxm, int nrhs) {
     return maxp <= NB && maxm <= kSmallMaxM && small_smem_bytes<T>(nrhs, maxm) <= kSmallSmemMax;
 }
 
-// Epoch of the next cooperative launch (never 0, the value flags start at).
-inline unsigned next_epoch(fdfd_factor *fac) {
-    if (++fac->epoch == 0) ++fac->epoch;
-    return fac->epoch;
-}
-
 template <typename T, typename R>
 int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
@@ -1880,13 +1908,11 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             GridBar *gb = (GridBar *)fac->d_bar;
             int *err = fac->d_solve_err;
             const int2 *units = fac->d_units + fac->unit_fwd_off[L];
-            int nunits = fac->unit_fwd_n[L], kpm = fac->lev_kp[L];
-            unsigned *flags = fac->d_flags;
-            unsigned epoch = next_epoch(fac);
+            int nunits = fac->unit_fwd_n[L];
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
                             (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err,
-                            (void *)&units, (void *)&nunits, (void *)&kpm, (void *)&flags, (void *)&epoch};
+                            (void *)&units, (void *)&nunits};
             // grid: the most work items any phase of this level has, capped
             // at the co-resident limit
             const int items = std::max(nfl, nunits);
@@ -1932,14 +1958,11 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             int *err = fac->d_solve_err;
             T *scr = (T *)fac->d_coop_scratch;
             const int2 *units = fac->d_units + fac->unit_bwd_off[L];
-            int nunits = fac->unit_bwd_n[L], kpm = fac->lev_kp[L];
-            unsigned *flags = fac->d_flags;
-            unsigned epoch = next_epoch(fac);
+            int nunits = fac->unit_bwd_n[L];
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxpp, (void *)&maxb,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
                             (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
-                            (void *)&gb, (void *)&err, (void *)&units, (void *)&nunits, (void *)&kpm,
-                            (void *)&flags, (void *)&epoch};
+                            (void *)&gb, (void *)&err, (void *)&units, (void *)&nunits};
             const int prw = (maxpp + kItemRows - 1) / kItemRows;
             const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
             const int items = std::max(std::max(nfl * prw * cch, nfl), nunits);
@@ -2053,7 +2076,7 @@ void free_factor(fdfd_factor *f) {
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
                     f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
                     f->d_bar, f->d_solve_err, f->d_coop_off, f->d_coop_scratch, f->d_krylov,
-                    f->d_units, f->d_flags, f->d_coef};
+                    f->d_units, f->d_coef};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (f->h_norm) cudaFreeHost(f->h_norm);
@@ -2149,12 +2172,10 @@ int64_t coop_layout(const Symbolic &S, int max_nrhs, std::vector<char> *lev, std
 // (rows p + 64 (R - KP) ...), sorted by R; backward list: pivot blocks sorted
 // by KP - 1 - R.  A unit waits only on units of its own front that come
 // earlier in its list, so CTAs that take the units in list order (all CTAs
-// co-resident) always make progress.  Returns the number of flags needed
-// (the most fronts x panels of any cooperative level).
+// co-resident) always make progress.
 struct PipeLayout {
     std::vector<int2> units;
-    std::vector<int> fwd_off, fwd_n, bwd_off, bwd_n, kp;
-    int64_t flags = 0;
+    std::vector<int> fwd_off, fwd_n, bwd_off, bwd_n;
 };
 PipeLayout pipe_layout(const Symbolic &S) {
     PipeLayout pl;
@@ -2162,13 +2183,10 @@ PipeLayout pipe_layout(const Symbolic &S) {
     pl.fwd_n.assign(S.nlev, 0);
     pl.bwd_off.assign(S.nlev, 0);
     pl.bwd_n.assign(S.nlev, 0);
-    pl.kp.assign(S.nlev, 0);
     for (int L = 0; L < S.nlev; ++L) {
         const int kpm = (S.lev_max_p[L] + NB - 1) / NB;
         if (kpm < kCoopPanels) continue;
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
-        pl.kp[L] = kpm;
-        pl.flags = std::max<int64_t>(pl.flags, (int64_t)nfl * kpm);
         int rmax = 0;
         for (int f = fb; f < fb + nfl; ++f)
             rmax = std::max(rmax, (S.p[f] + NB - 1) / NB + (S.m[f] - S.p[f] + NB - 1) / NB);
@@ -2205,7 +2223,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
     b += coop_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8 + 16;
     const PipeLayout pl = pipe_layout(S);
-    b += (int64_t)pl.units.size() * sizeof(int2) + pl.flags * 4;
+    b += (int64_t)pl.units.size() * sizeof(int2);
     return b;
 }
 
@@ -2363,14 +2381,11 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
             f->unit_fwd_n = pl.fwd_n;
             f->unit_bwd_off = pl.bwd_off;
             f->unit_bwd_n = pl.bwd_n;
-            f->lev_kp = pl.kp;
-            if (!alloc((void **)&f->d_units, pl.units.size() * sizeof(int2)) ||
-                !alloc((void **)&f->d_flags, pl.flags * sizeof(unsigned))) {
+            if (!alloc((void **)&f->d_units, pl.units.size() * sizeof(int2))) {
                 free_factor(f);
                 return fail(FDFD_ERR_OOM, "factor_create: pipelined-solve allocation failed");
             }
             e = cudaMemcpy(f->d_units, pl.units.data(), pl.units.size() * sizeof(int2), cudaMemcpyHostToDevice);
-            if (e == cudaSuccess) e = cudaMemset(f->d_flags, 0, std::max<int64_t>(pl.flags, 1) * sizeof(unsigned));
             if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
         }
     }
