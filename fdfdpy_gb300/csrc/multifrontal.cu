@@ -319,55 +319,74 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
         const int kw = min(kStep, P - c0), b1 = c0 + kw;
         if (tid == 0) lu4_inv<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
         __syncthreads();
-        // L21 rows [b1, S): l = a inv(U11);  U12 columns [b1, S): u = inv(L11) a
+        // L21 rows [b1, S): l = a inv(U11) (threads 0-127);  U12 columns
+        // [b1, S): u = inv(L11) a (threads 128-255), so each warp runs one
+        // of the two loops
         const int nr = S - b1;
-        for (int item = tid; item < 2 * nr; item += kDenseThreads) {
-            const bool is_row = item < nr;
-            const int idx = b1 + (is_row ? item : item - nr);
-            T *base = is_row ? D + idx + c0 * LD : D + c0 + idx * LD;
-            const int step = is_row ? LD : 1;
-            T v[kStep];
+        if (tid < kDenseThreads / 2) {
+            for (int idx = b1 + tid; idx < S; idx += kDenseThreads / 2) {
+                T *base = D + idx + c0 * LD;
+                T v[kStep];
 #pragma unroll
-            for (int j = 0; j < kStep; ++j) v[j] = (j < kw) ? base[j * step] : czero<T>();
+                for (int j = 0; j < kStep; ++j) v[j] = (j < kw) ? base[j * LD] : czero<T>();
 #pragma unroll
-            for (int j = 0; j < kStep; ++j) {
-                T s = is_row ? czero<T>() : v[j];
+                for (int j = 0; j < kStep; ++j) {
+                    T s = czero<T>();
 #pragma unroll
-                for (int k = 0; k < kStep; ++k) {
-                    if (is_row && k <= j) cmac(s, v[k], D[(c0 + k) + (c0 + j) * LD]);
-                    if (!is_row && k < j) cmac(s, D[(c0 + j) + (c0 + k) * LD], v[k]);
+                    for (int k = 0; k <= j; ++k) cmac(s, v[k], D[(c0 + k) + (c0 + j) * LD]);
+                    if (j < kw) base[j * LD] = s;
                 }
-                if (j < kw) base[j * step] = s;
+            }
+        } else {
+            for (int idx = b1 + tid - kDenseThreads / 2; idx < S; idx += kDenseThreads / 2) {
+                T *base = D + c0 + idx * LD;
+                T v[kStep];
+#pragma unroll
+                for (int j = 0; j < kStep; ++j) v[j] = (j < kw) ? base[j] : czero<T>();
+#pragma unroll
+                for (int j = 0; j < kStep; ++j) {
+                    T s = v[j];
+#pragma unroll
+                    for (int k = 0; k < j; ++k) cmac(s, D[(c0 + j) + (c0 + k) * LD], v[k]);
+                    if (j < kw) base[j] = s;
+                }
             }
         }
+        (void)nr;
         __syncthreads();
-        // trailing rows / columns [b1, S) -= L21 U12 (rank kw)
+        // trailing rows / columns [b1, S) -= L21 U12 (rank kw).  Rows and
+        // columns of the 16-blocks that lie before b1 take zero multipliers,
+        // so their read-modify-write leaves them unchanged and the entry loop
+        // needs only the block bounds, which are the same across a warp.
         const int Ilo = b1 / 16;
         for (int I0 = Ilo; I0 < NBLK; I0 += 4)
             for (int J0 = Ilo; J0 < NBLK; J0 += 4) {
                 T l[4][kStep], u[kStep][4];
 #pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 16 * (I0 + i) + tx;
+                    const bool rl = I0 + i < NBLK && r >= b1;
+#pragma unroll
+                    for (int k = 0; k < kStep; ++k) l[i][k] = (rl && k < kw) ? D[r + (c0 + k) * LD] : czero<T>();
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int c = 16 * (J0 + j) + ty;
+                    const bool cl = J0 + j < NBLK && c >= b1;
+#pragma unroll
+                    for (int k = 0; k < kStep; ++k) u[k][j] = (cl && k < kw) ? D[(c0 + k) + c * LD] : czero<T>();
+                }
+#pragma unroll
                 for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int k = 0; k < kStep; ++k)
-                        l[i][k] = (I0 + i < NBLK && k < kw) ? D[(16 * (I0 + i) + tx) + (c0 + k) * LD] : czero<T>();
-#pragma unroll
-                for (int k = 0; k < kStep; ++k)
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
-                        u[k][j] = (J0 + j < NBLK && k < kw) ? D[(c0 + k) + (16 * (J0 + j) + ty) * LD] : czero<T>();
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int r = 16 * (I0 + i) + tx, c = 16 * (J0 + j) + ty;
-                        if (I0 + i < NBLK && J0 + j < NBLK && r >= b1 && c >= b1) {
-                            T acc = D[r + c * LD];
+                        if (I0 + i < NBLK && J0 + j < NBLK) {
+                            const int e = (16 * (I0 + i) + tx) + (16 * (J0 + j) + ty) * LD;
+                            T acc = D[e];
 #pragma unroll
                             for (int k = 0; k < kStep; ++k) cmsub(acc, l[i][k], u[k][j]);
-                            D[r + c * LD] = acc;
+                            D[e] = acc;
                         }
-                    }
             }
         __syncthreads();
     }
