@@ -283,7 +283,10 @@ __device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_
 
 // complex64: at most 80 registers so that three CTAs share an SM (the
 // leaves' fronts are latency-bound; 2 CTAs per SM ran 1.7x slower there).
-template <typename T, typename R>
+// SC > 0 fixes the padded size S at compile time (every block of the launch
+// has n <= SC), so that the shared-memory offsets fold into the addressing;
+// SC = 0 takes S from each block.
+template <typename T, typename R, int SC>
 __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
                                                             int k0, int whole, R tiny, int *tiny_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     }
     if (P <= 0 || n <= 0) return;
     const int64_t ld = f.ld;
-    const int S = (n + 15) / 16 * 16, LD = S + 1, NBLK = S / 16;
+    const int S = SC > 0 ? SC : (n + 15) / 16 * 16, LD = S + 1, NBLK = S / 16;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int c = warp; c < S; c += kDenseThreads / 32)
         for (int r = lane; r < S; r += 32) {
@@ -460,6 +463,25 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     }
     for (int c = warp; c < n; c += kDenseThreads / 32)
         for (int r = lane; r < n; r += 32) G[r + (int64_t)c * ld] = D[r + c * LD];
+}
+
+// Launch k_dense_lu for blocks padded to S.  The 64-wide panel blocks and
+// the leaves' 80-row fronts have their own builds (about 10% faster there;
+// larger fixed sizes ran slower than the generic build).
+template <typename T, typename R>
+void dense_lu_launch(int nfl, int S, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0, int whole, R tiny,
+                     int *tiny_count) {
+    const size_t smem = dense_lu_smem<T>(S);
+    switch (S) {
+    case 64:
+        k_dense_lu<T, R, 64><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+        break;
+    case 80:
+        k_dense_lu<T, R, 80><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+        break;
+    default:
+        k_dense_lu<T, R, 0><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+    }
 }
 
 enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
@@ -1379,8 +1401,7 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
     cudaStream_t s2 = fac->st_look;
     constexpr int kNextTiles = NB / kTileNc;  // column tiles of the next panel
     prof_begin(PROF_LU_DIAG, st);
-    k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), st>>>(fac->d_fronts, pool, fb, 0, 0, tiny,
-                                                                        fac->d_tiny);
+    dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, 0, 0, tiny, fac->d_tiny);
     prof_end(PROF_LU_DIAG, st, 1);
     for (int k0 = 0; k0 < maxp; k0 += NB) {
         const int trail = maxm - k0 - 1;  // upper bound of m - t0
@@ -1400,8 +1421,7 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
             CUDA_TRY(cudaEventRecord(fac->ev_look[0], st));
             CUDA_TRY(cudaStreamWaitEvent(s2, fac->ev_look[0], 0));
             prof_begin(PROF_LU_DIAG, s2);
-            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), s2>>>(fac->d_fronts, pool, fb, k0 + NB, 0,
-                                                                                tiny, fac->d_tiny);
+            dense_lu_launch<T, R>(nfl, NB, s2, fac->d_fronts, pool, fb, k0 + NB, 0, tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, s2, 1);
             CUDA_TRY(cudaEventRecord(fac->ev_look[1], s2));
         }
@@ -1457,8 +1477,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         if (dense_front_fits<T>(fac, maxp, maxm)) {
             // every front of the level in one launch: LU, L21, U12 and the update matrix
             prof_begin(PROF_LU_DIAG, st);
-            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(maxm), st>>>(fac->d_fronts, pool, fb, 0, 1,
-                                                                                  tiny, fac->d_tiny);
+            dense_lu_launch<T, R>(nfl, (maxm + 15) / 16 * 16, st, fac->d_fronts, pool, fb, 0, 1, tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             continue;
         }
@@ -1470,8 +1489,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         }
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
-            k_dense_lu<T, R><<<nfl, kDenseThreads, dense_lu_smem<T>(NB), st>>>(fac->d_fronts, pool, fb, k0, 0,
-                                                                                tiny, fac->d_tiny);
+            dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, k0, 0, tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             const int trail = maxm - k0 - 1;  // upper bound of m - t0
             if (trail <= 0) continue;
@@ -1883,8 +1901,13 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
 
 template <typename T, typename R>
 int set_smem_attrs() {
-    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDenseSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 80>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDenseSmemMax));
+
     const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
