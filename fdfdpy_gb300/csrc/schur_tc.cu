@@ -171,8 +171,7 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 //     read straight from the front) into tensor memory -- thread = TMEM
 //     lane = row -- so the MMAs read A from TMEM and only B from shared
 //     memory; then they drain the accumulators (tcgen05.ld, C -= acc), the
-//     next tile's C entries already loading (eight warps keep twice the C
-//     loads in flight of four);
+//     next two tiles' C entries already loading;
 //   warp 9 (lane 0) streams the B'' tiles (hi, lo) through kStages shared-
 //     memory stages, refilling a stage once the MMAs that read it are done;
 //   warp 8 (lane 0) issues the 48 MMAs of each column tile (16 K-steps x 3)
@@ -325,22 +324,24 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(bar_a);
 
-        c64 cv[kHalf], nv[kHalf];
+        // C entries of this tile (cv) and of the next two (nv, nnv) are in
+        // flight while the MMAs finish
+        c64 cv[kHalf], nv[kHalf], nnv[kHalf];
 #pragma unroll
         for (int q = 0; q < kHalf; ++q) {
             const int col = t0 + ct0 * kTileNc + kHalf * h + q;
             cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
-            nv[q] = czero<c64>();
+            nv[q] = (live && J > 1 && col + kTileNc < f.m) ? F[row + (int64_t)(col + kTileNc) * ld] : czero<c64>();
+            nnv[q] = czero<c64>();
         }
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
             const int colbase = t0 + (ct0 + j) * kTileNc + kHalf * h;
-            // the next tile's C entries load while this tile's MMAs finish
-            if (j + 1 < J) {
+            if (j + 2 < J) {
 #pragma unroll
                 for (int q = 0; q < kHalf; ++q) {
-                    const int col = colbase + kTileNc + q;
-                    nv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+                    const int col = colbase + 2 * kTileNc + q;
+                    nnv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
                 }
             }
             const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
@@ -372,7 +373,10 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kHalf; ++q) cv[q] = nv[q];
+            for (int q = 0; q < kHalf; ++q) {
+                cv[q] = nv[q];
+                nv[q] = nnv[q];
+            }
         }
     }
     tc_fence_before();
