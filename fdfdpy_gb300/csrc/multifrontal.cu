@@ -520,45 +520,62 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
 #pragma unroll
         for (int b = 0; b < 4; ++b) acc[a][b] = czero<T>();
 
+    // The A and B elements of K chunk kc + BK load into registers while
+    // chunk kc is multiplied out of shared memory.
+    auto load_a = [&](int kc, int q) -> T {
+        const int idx = tid + 256 * q;
+        const int rr = idx % BM, kk = idx / BM;
+        const int r = rbase + rr, kg = kc + kk;
+        T v = czero<T>();
+        if (r < rend && kg < w) {
+            if (MODE == TRSM_U) {
+                // unit lower inv(L_kk): rows are k0 + rr
+                const int lr = rr;
+                if (kg < lr) v = F[(k0 + lr) + (int64_t)(k0 + kg) * ld];
+                else if (kg == lr) v = cone<T>();
+            } else {
+                v = F[r + (int64_t)(k0 + kg) * ld];
+            }
+        }
+        return v;
+    };
+    auto load_b = [&](int kc, int q) -> T {
+        const int idx = tid + 256 * q;
+        const int kk = idx % BK, cc = idx / BK;
+        const int c = cbase + cc, kg = kc + kk;
+        T v = czero<T>();
+        if (c < cend && kg < w) {
+            if (MODE == TRSM_L) {
+                // upper inv(U_kk): cols are k0 + (c - k0)
+                const int uc = c - k0;
+                if (kg <= uc) v = F[(k0 + kg) + (int64_t)c * ld];
+            } else {
+                v = F[(k0 + kg) + (int64_t)c * ld];
+            }
+        }
+        return v;
+    };
+    T pa[4], pb[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        pa[q] = load_a(0, q);
+        pb[q] = load_b(0, q);
+    }
     for (int kc = 0; kc < w; kc += BK) {
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int idx = tid + 256 * q;
-            // A tile element (row rr, k kk)
-            {
-                const int rr = idx % BM, kk = idx / BM;
-                const int r = rbase + rr, kg = kc + kk;
-                T v = czero<T>();
-                if (r < rend && kg < w) {
-                    if (MODE == TRSM_U) {
-                        // unit lower inv(L_kk): rows are k0 + rr
-                        const int lr = rr;
-                        if (kg < lr) v = F[(k0 + lr) + (int64_t)(k0 + kg) * ld];
-                        else if (kg == lr) v = cone<T>();
-                    } else {
-                        v = F[r + (int64_t)(k0 + kg) * ld];
-                    }
-                }
-                As[kk][rr] = v;
-            }
-            // B tile element (k kk, col cc)
-            {
-                const int kk = idx % BK, cc = idx / BK;
-                const int c = cbase + cc, kg = kc + kk;
-                T v = czero<T>();
-                if (c < cend && kg < w) {
-                    if (MODE == TRSM_L) {
-                        // upper inv(U_kk): cols are k0 + (c - k0)
-                        const int uc = c - k0;
-                        if (kg <= uc) v = F[(k0 + kg) + (int64_t)c * ld];
-                    } else {
-                        v = F[(k0 + kg) + (int64_t)c * ld];
-                    }
-                }
-                Bs[kk][cc] = v;
-            }
+            As[idx / BM][idx % BM] = pa[q];
+            Bs[idx % BK][idx / BK] = pb[q];
         }
         __syncthreads();
+        if (kc + BK < w) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                pa[q] = load_a(kc + BK, q);
+                pb[q] = load_b(kc + BK, q);
+            }
+        }
         // the triangular inverses are zero below (inv(U), TRSM_L) or above
         // (inv(L), TRSM_U) their diagonal: K chunk kc adds nothing to the
         // output columns (rows) of the 16-blocks before it
@@ -628,7 +645,7 @@ __global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ f
 // forms L (row tile blockIdx.y), blockIdx.z = 1 forms U (column tile
 // blockIdx.y) and, on tensor-core levels (tcf != NULL), its packed tiles.
 template <typename T, typename R>
-__global__ void __launch_bounds__(256) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
                                                     const TcFront *__restrict__ tcf, uint8_t *scratch) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
