@@ -199,11 +199,17 @@ __host__ __device__ __forceinline__ size_t dense_lu_smem(int n) {
     return (size_t)S * (S + 1) * sizeof(T);
 }
 
-// 1/b = conj(b) / |b|^2 with a round-to-nearest reciprocal; the operands are
-// pivots of the operator scaled to max|diag| = 1 and at least the static
-// pivot threshold, so |b|^2 stays inside the normal range.
+// 1/b = conj(b) / |b|^2; the operands are pivots of the operator scaled to
+// max|diag| = 1 and at least the static pivot threshold, so |b|^2 stays
+// inside the normal range.  complex64: the hardware reciprocal estimate
+// refined by one Newton-Raphson step, r' = r (2 - x r) (within an ulp of
+// 1/x, and off the serial 4 x 4 step's latency compared with a
+// correctly rounded reciprocal).
 __device__ __forceinline__ c64 crecip_fast(c64 b) {
-    const float s = __frcp_rn(fmaf(b.x, b.x, b.y * b.y));
+    const float x = fmaf(b.x, b.x, b.y * b.y);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    const float s = r * fmaf(-x, r, 2.0f);
     return cmake<float>(b.x * s, -b.y * s);
 }
 __device__ __forceinline__ c128 crecip_fast(c128 b) {
@@ -285,10 +291,13 @@ __device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_
 // leaves' fronts are latency-bound; 2 CTAs per SM ran 1.7x slower there).
 // SC > 0 fixes the padded size S at compile time (every block of the launch
 // has n <= SC), so that the shared-memory offsets fold into the addressing;
-// SC = 0 takes S from each block.
+// SC = 0 takes S from each block.  blocked != 0 (whole fronts of the levels
+// solved one warp per front) completes the inverses only inside the 16 x 16
+// diagonal blocks of the pivot block and keeps L and U below / above them:
+// the warp substitutions work block by block.
 template <typename T, typename R, int SC>
 __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
-                                                            int k0, int whole, R tiny, int *tiny_count) {
+                                                            int k0, int whole, int blocked, R tiny, int *tiny_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *D = reinterpret_cast<T *>(smem_raw);
     const FrontD f = fr[f_begin + blockIdx.x];
@@ -401,11 +410,14 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     const int q = tid & 3, g = tid >> 2;  // 64 groups of four threads
     for (int B = 1; B < nb4; ++B) {
         const int b0 = B * kStep, bs = min(kStep, P - b0);
+        // blocked: only columns (rows) of b0's 16-block take part
+        const int glo = blocked ? (b0 & ~15) : 0;
+        if (glo == b0) continue;
         T vl[kStep], vu[kStep];
         // lower: groups g < b0 take column g; upper: groups g < b0 take row g
 #pragma unroll
         for (int i = 0; i < kStep; ++i) vl[i] = vu[i] = czero<T>();
-        if (g < b0) {
+        if (g < b0 && g >= glo) {
             const int col = g;
             for (int k = col + 1 + q; k < b0; k += 4) {
                 const T x = D[k + col * LD];
@@ -429,7 +441,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
             }
         // X[B, col] = -inv(L_BB) (L[B, col] + sum), Y[row, B] = -(sum) inv(U_BB)
         T xo[kStep], yo[kStep];
-        if (g < b0 && q == 0) {
+        if (g < b0 && g >= glo && q == 0) {
             const int col = g;
 #pragma unroll
             for (int i = 0; i < kStep; ++i)
@@ -450,7 +462,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
             }
         }
         __syncthreads();
-        if (g < b0 && q == 0) {
+        if (g < b0 && g >= glo && q == 0) {
             const int col = g, row = g;
 #pragma unroll
             for (int i = 0; i < kStep; ++i)
@@ -469,18 +481,18 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
 // the leaves' 80-row fronts have their own builds (about 10% faster there;
 // larger fixed sizes ran slower than the generic build).
 template <typename T, typename R>
-void dense_lu_launch(int nfl, int S, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0, int whole, R tiny,
-                     int *tiny_count) {
+void dense_lu_launch(int nfl, int S, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0, int whole,
+                     int blocked, R tiny, int *tiny_count) {
     const size_t smem = dense_lu_smem<T>(S);
     switch (S) {
     case 64:
-        k_dense_lu<T, R, 64><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+        k_dense_lu<T, R, 64><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
         break;
     case 80:
-        k_dense_lu<T, R, 80><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+        k_dense_lu<T, R, 80><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
         break;
     default:
-        k_dense_lu<T, R, 0><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, tiny, tiny_count);
+        k_dense_lu<T, R, 0><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
     }
 }
 
@@ -826,10 +838,100 @@ __host__ __device__ __forceinline__ size_t warp_smem_bytes(int nrhs, int maxm) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kWarpFronts)
+__device__ __forceinline__ T pick4(const T (&a)[4], int k) {
+    return k == 0 ? a[0] : k == 1 ? a[1] : k == 2 ? a[2] : a[3];
+}
+
+// Blocked forward substitution of one front by one warp (blocked pivot-
+// block format): w (shared, length m) holds the gathered right-hand side;
+// the pivot rows R_k = lane + 32 k (k < 2, p <= 64) accumulate in acc[k].
+// Per 16-block I of the pivots: the block's accumulated values go through
+// w, each block lane forms y_r = acc_r + sum_{c0 <= c < r} inv(L_II)[r, c]
+// acc_c, and the pivot rows of later blocks take acc_R -= L[R, I] y_I.  On
+// return w[0, p) holds y (the update rows are formed afterwards in one pass
+// over L21, as with the full inverse).
+template <typename T>
+__device__ __forceinline__ void warp_fwd_blocked(const T *F, int64_t ld, int p, T *w, int lane) {
+    T acc[4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int R = lane + 32 * k;
+        acc[k] = R < p ? w[R] : czero<T>();
+    }
+    acc[2] = acc[3] = czero<T>();
+    for (int c0 = 0; c0 < p; c0 += 16) {
+        const int cw = min(16, p - c0), kI = c0 >> 5, l0 = c0 & 31;
+        const bool inb = lane >= l0 && lane < l0 + cw;
+        const int r = c0 + lane - l0;
+        if (inb) w[r] = pick4(acc, kI);
+        __syncwarp();
+        T y = czero<T>();
+        if (inb) {
+            y = w[r];
+#pragma unroll
+            for (int j = 0; j < 15; ++j)
+                if (c0 + j < r) cmac(y, F[r + (int64_t)(c0 + j) * ld], w[c0 + j]);
+        }
+        __syncwarp();
+        if (inb) w[r] = y;
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int R = lane + 32 * k;
+            if (k == kI && inb) acc[k] = y;
+            if (R >= c0 + cw && R < p) {
+                T sum = czero<T>();
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (j < cw) cmac(sum, F[R + (int64_t)(c0 + j) * ld], w[c0 + j]);
+                acc[k] = csub(acc[k], sum);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// Blocked backward substitution (blocked format): on entry acc[k] holds
+// y_R - U12[R, :] x_B for the pivot rows R = lane + 32 k < p.  Per 16-block
+// I from the last: x_I = inv(U_II) acc_I through xr, then every earlier
+// pivot row takes acc_R -= U[R, I] x_I.  On return xr[0, p) holds x_P.
+template <typename T>
+__device__ __forceinline__ void warp_bwd_blocked(const T *F, int64_t ld, int p, T *xr, int lane, T (&acc)[4]) {
+    for (int c0 = (p - 1) & ~15; c0 >= 0; c0 -= 16) {
+        const int cw = min(16, p - c0), kI = c0 >> 5, l0 = c0 & 31;
+        const bool inb = lane >= l0 && lane < l0 + cw;
+        const int r = c0 + lane - l0;
+        if (inb) xr[r] = pick4(acc, kI);
+        __syncwarp();
+        T xv = czero<T>();
+        if (inb) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (j < cw && c0 + j >= r) cmac(xv, F[r + (int64_t)(c0 + j) * ld], xr[c0 + j]);
+        }
+        __syncwarp();
+        if (inb) xr[r] = xv;
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int R = lane + 32 * k;
+            if (R < c0) {
+                T sum = czero<T>();
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (j < cw) cmac(sum, F[R + (int64_t)(c0 + j) * ld], xr[c0 + j]);
+                acc[k] = csub(acc[k], sum);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpFronts, 4)
     k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
-               int nrhs, int f_begin, int nfl, int maxm) {
+               int nrhs, int f_begin, int nfl, int maxm, int blocked) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int fi = blockIdx.x * kWarpFronts + warp;
@@ -858,26 +960,33 @@ __global__ void __launch_bounds__(32 * kWarpFronts)
     const int r0 = lane, r1 = lane + 32;
     for (int r = 0; r < nrhs; ++r) {
         T *w = ws + r * maxm;
+        if (blocked) {
+            warp_fwd_blocked(F, ld, p, w, lane);
+            if (r0 < p) Y[r * sum_m + f.voff + r0] = w[r0];
+            if (r1 < p) Y[r * sum_m + f.voff + r1] = w[r1];
+        }
         // y = inv(L11) w_P: y_i = w_i + sum_{t<i} invL[i][t] w_t (rows r0, r1 < p <= 64)
         T a0 = czero<T>(), a1 = czero<T>();
+        if (!blocked) {
 #pragma unroll 8
-        for (int t = 0; t < p; ++t) {
-            const T wt = w[t];
-            if (t < r0) cmac(a0, F[r0 + (int64_t)t * ld], wt);
-            if (t < r1 && r1 < p) cmac(a1, F[r1 + (int64_t)t * ld], wt);
+            for (int t = 0; t < p; ++t) {
+                const T wt = w[t];
+                if (t < r0) cmac(a0, F[r0 + (int64_t)t * ld], wt);
+                if (t < r1 && r1 < p) cmac(a1, F[r1 + (int64_t)t * ld], wt);
+            }
+            __syncwarp();
+            if (r0 < p) {
+                const T y = cadd(w[r0], a0);
+                w[r0] = y;
+                Y[r * sum_m + f.voff + r0] = y;
+            }
+            if (r1 < p) {
+                const T y = cadd(w[r1], a1);
+                w[r1] = y;
+                Y[r * sum_m + f.voff + r1] = y;
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        if (r0 < p) {
-            const T y = cadd(w[r0], a0);
-            w[r0] = y;
-            Y[r * sum_m + f.voff + r0] = y;
-        }
-        if (r1 < p) {
-            const T y = cadd(w[r1], a1);
-            w[r1] = y;
-            Y[r * sum_m + f.voff + r1] = y;
-        }
-        __syncwarp();
         // update rows: w_B -= L21 y
         for (int rb = p; rb < m; rb += 32) {
             const int row = rb + lane;
@@ -893,10 +1002,10 @@ __global__ void __launch_bounds__(32 * kWarpFronts)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kWarpFronts)
+__global__ void __launch_bounds__(32 * kWarpFronts, 4)
     k_bwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const T *__restrict__ pool,
                const T *__restrict__ Y, double2 *x, int64_t sum_m, int64_t n, int nrhs, int f_begin, int nfl,
-               int maxm) {
+               int maxm, int blocked) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int fi = blockIdx.x * kWarpFronts + warp;
@@ -920,6 +1029,17 @@ __global__ void __launch_bounds__(32 * kWarpFronts)
             const T xc = xr[c];
             if (r0 < p) cmac(a0, F[r0 + (int64_t)c * ld], xc);
             if (r1 < p) cmac(a1, F[r1 + (int64_t)c * ld], xc);
+        }
+        if (blocked) {
+            T acc[4];
+            acc[0] = r0 < p ? csub(Y[r * sum_m + f.voff + r0], a0) : czero<T>();
+            acc[1] = r1 < p ? csub(Y[r * sum_m + f.voff + r1], a1) : czero<T>();
+            acc[2] = acc[3] = czero<T>();
+            warp_bwd_blocked(F, ld, p, xr, lane, acc);
+            if (r0 < p) x[r * n + v[r0]] = to_c128(xr[r0], 1.0);
+            if (r1 < p) x[r * n + v[r1]] = to_c128(xr[r1], 1.0);
+            __syncwarp();
+            continue;
         }
         if (r0 < p) xr[r0] = csub(Y[r * sum_m + f.voff + r0], a0);
         if (r1 < p) xr[r1] = csub(Y[r * sum_m + f.voff + r1], a1);
@@ -1381,6 +1501,9 @@ struct fdfd_factor {
     // tensor-core Schur path (FDFD_PREC_C64_TC)
     bool use_tc = false;
     std::vector<char> tc_level;
+    // levels whose pivot blocks hold the blocked format (16 x 16 diagonal-
+    // block inverses, L and U elsewhere; set by each factorization)
+    std::vector<char> blocked_level;
     TcFront *d_tcf = nullptr;
     uint8_t *d_scratch = nullptr;
     int *d_tcerr = nullptr;
@@ -1418,7 +1541,7 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
     cudaStream_t s2 = fac->st_look;
     constexpr int kNextTiles = NB / kTileNc;  // column tiles of the next panel
     prof_begin(PROF_LU_DIAG, st);
-    dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, 0, 0, tiny, fac->d_tiny);
+    dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, 0, 0, 0, tiny, fac->d_tiny);
     prof_end(PROF_LU_DIAG, st, 1);
     for (int k0 = 0; k0 < maxp; k0 += NB) {
         const int trail = maxm - k0 - 1;  // upper bound of m - t0
@@ -1438,7 +1561,7 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
             CUDA_TRY(cudaEventRecord(fac->ev_look[0], st));
             CUDA_TRY(cudaStreamWaitEvent(s2, fac->ev_look[0], 0));
             prof_begin(PROF_LU_DIAG, s2);
-            dense_lu_launch<T, R>(nfl, NB, s2, fac->d_fronts, pool, fb, k0 + NB, 0, tiny, fac->d_tiny);
+            dense_lu_launch<T, R>(nfl, NB, s2, fac->d_fronts, pool, fb, k0 + NB, 0, 0, tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, s2, 1);
             CUDA_TRY(cudaEventRecord(fac->ev_look[1], s2));
         }
@@ -1471,6 +1594,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     const double def = std::is_same<R, float>::value ? 1e-5 : std::sqrt((double)std::numeric_limits<R>::epsilon());
     const R tiny = (R)(fac->pivot_tol >= 0.0 ? fac->pivot_tol : def);
     T *pool = (T *)fac->d_pool;
+    fac->blocked_level.assign(S.nlev, 0);
     for (int L = 0; L < S.nlev; ++L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
         if (L > 0) {
@@ -1494,7 +1618,11 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         if (dense_front_fits<T>(fac, maxp, maxm)) {
             // every front of the level in one launch: LU, L21, U12 and the update matrix
             prof_begin(PROF_LU_DIAG, st);
-            dense_lu_launch<T, R>(nfl, (maxm + 15) / 16 * 16, st, fac->d_fronts, pool, fb, 0, 1, tiny, fac->d_tiny);
+            // levels solved one warp per front keep the blocked pivot-block format
+            const int blocked = maxm <= kWarpMaxM ? 1 : 0;
+            fac->blocked_level[L] = (char)blocked;
+            dense_lu_launch<T, R>(nfl, (maxm + 15) / 16 * 16, st, fac->d_fronts, pool, fb, 0, 1, blocked, tiny,
+                                  fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             continue;
         }
@@ -1506,7 +1634,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         }
         for (int k0 = 0; k0 < maxp; k0 += NB) {
             prof_begin(PROF_LU_DIAG, st);
-            dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, k0, 0, tiny, fac->d_tiny);
+            dense_lu_launch<T, R>(nfl, NB, st, fac->d_fronts, pool, fb, k0, 0, 0, tiny, fac->d_tiny);
             prof_end(PROF_LU_DIAG, st, 1);
             const int trail = maxm - k0 - 1;  // upper bound of m - t0
             if (trail <= 0) continue;
@@ -1985,7 +2113,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         if (warp_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
                             st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, nfl,
-                                  maxm);
+                                  maxm, (int)fac->blocked_level[L]);
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
@@ -2034,7 +2162,8 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         if (warp_level_fits<T>(maxp, S.lev_max_m[L], nrhs)) {
             const int maxm = S.lev_max_m[L];
             k_bwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
-                            st>>>(fac->d_fronts, fac->d_vars, pool, Y, x, sum_m, n, nrhs, fb, nfl, maxm);
+                            st>>>(fac->d_fronts, fac->d_vars, pool, Y, x, sum_m, n, nrhs, fb, nfl, maxm,
+                                  (int)fac->blocked_level[L]);
             prof_end(PROF_SOLVE_BWD, st, 1);
             continue;
         }

@@ -171,7 +171,8 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 //     read straight from the front) into tensor memory -- thread = TMEM
 //     lane = row -- so the MMAs read A from TMEM and only B from shared
 //     memory; then they drain the accumulators (tcgen05.ld, C -= acc), the
-//     next two tiles' C entries already loading;
+//     next tile's C entries already loading (eight warps keep twice the C
+//     loads in flight of four);
 //   warp 9 (lane 0) streams the B'' tiles (hi, lo) through kStages shared-
 //     memory stages, refilling a stage once the MMAs that read it are done;
 //   warp 8 (lane 0) issues the 48 MMAs of each column tile (16 K-steps x 3)
@@ -196,7 +197,10 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-__global__ void __launch_bounds__(kCtaThreads, 1)
+// At most 128 registers a thread (one CTA: 40,960) so that a 256-thread,
+// 80-register diagonal-block LU of the look-ahead stream (20,480) fits on
+// the same SM beside it; shared memory fits likewise (196.9 + 33.3 KB).
+__global__ void __maxnreg__(128)
     k_schur_tc(const TcFront *__restrict__ fr, c64 *pool, int f_begin, int k0, int ct_lo, int ct_hi,
                const uint8_t *scratch, int *err) {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -324,24 +328,22 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(bar_a);
 
-        // C entries of this tile (cv) and of the next two (nv, nnv) are in
-        // flight while the MMAs finish
-        c64 cv[kHalf], nv[kHalf], nnv[kHalf];
+        c64 cv[kHalf], nv[kHalf];
 #pragma unroll
         for (int q = 0; q < kHalf; ++q) {
             const int col = t0 + ct0 * kTileNc + kHalf * h + q;
             cv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
-            nv[q] = (live && J > 1 && col + kTileNc < f.m) ? F[row + (int64_t)(col + kTileNc) * ld] : czero<c64>();
-            nnv[q] = czero<c64>();
+            nv[q] = czero<c64>();
         }
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
             const int colbase = t0 + (ct0 + j) * kTileNc + kHalf * h;
-            if (j + 2 < J) {
+            // the next tile's C entries load while this tile's MMAs finish
+            if (j + 1 < J) {
 #pragma unroll
                 for (int q = 0; q < kHalf; ++q) {
-                    const int col = colbase + 2 * kTileNc + q;
-                    nnv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+                    const int col = colbase + kTileNc + q;
+                    nv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
                 }
             }
             const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
@@ -373,10 +375,7 @@ __global__ void __launch_bounds__(kCtaThreads, 1)
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kHalf; ++q) {
-                cv[q] = nv[q];
-                nv[q] = nnv[q];
-            }
+            for (int q = 0; q < kHalf; ++q) cv[q] = nv[q];
         }
     }
     tc_fence_before();
