@@ -108,11 +108,13 @@ __global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
                                   const int32_t *__restrict__ var_front,
                                   const int32_t *__restrict__ var_loc,
                                   const int32_t *__restrict__ nbr_loc,
-                                  const unsigned long long *maxdiag, T *pool) {
+                                  const unsigned long long *maxdiag, T *pool, int f_skip) {
     const int64_t n = (int64_t)o.Nx * o.Ny;
     const double sigma = 1.0 / __longlong_as_double((long long)*maxdiag);
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
          s += (int64_t)gridDim.x * blockDim.x) {
+        // fronts below f_skip (the leaves) are assembled by their LU kernel
+        if (var_front[s] < f_skip) continue;
         const int i = (int)(s / o.Ny), j = (int)(s % o.Ny);
         const FrontD f = fr[var_front[s]];
         T *F = pool + f.f_off;
@@ -295,9 +297,40 @@ __device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_
 // solved one warp per front) completes the inverses only inside the 16 x 16
 // diagonal blocks of the pivot block and keeps L and U below / above them:
 // the warp substitutions work block by block.
-template <typename T, typename R, int SC>
+// Row k and the boundary entries of column k of pivot k (operator row of
+// variable sv, scaled by 1/max|diag A|) into the shared-memory front D, as
+// k_assemble_fronts writes them into the pool; one thread writes each entry.
+template <typename T>
+__device__ __forceinline__ void assemble_pivot(const OpDev &o, int sv, int k, int P, const int32_t *__restrict__ nbr_loc,
+                                            const unsigned long long *maxdiag, T *D, int LD) {
+    const double sigma = 1.0 / __longlong_as_double((long long)*maxdiag);
+    const int i = sv / o.Ny, j = sv % o.Ny;
+    double2 c[5];
+    stencil_row(o, i, j, c);
+    D[k + k * LD] = cadd(D[k + k * LD], from_c128<T>(c[0], sigma));
+    for (int d = 0; d < 4; ++d) {
+        const int nl = nbr_loc[4 * (int64_t)sv + d];
+        if (nl < 0) continue;
+        D[k + nl * LD] = cadd(D[k + nl * LD], from_c128<T>(c[1 + d], sigma));
+        if (nl >= P) {
+            const int t = nbr_cell(o, i, j, d);
+            double2 ct[5];
+            stencil_row(o, t / o.Ny, t % o.Ny, ct);
+            D[nl + k * LD] = cadd(D[nl + k * LD], from_c128<T>(ct[1 + opposite_dir(d)], sigma));
+        }
+    }
+}
+
+// ASM (the leaves' builds): the front is assembled here, in shared memory,
+// from the operator's rows of its pivot variables (as k_assemble_fronts
+// would write them) instead of being read from the pool; a separate build
+// so that the other builds keep their register allocation.
+template <typename T, typename R, int SC, bool ASM>
 __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense_lu(const FrontD *__restrict__ fr, T *pool, int f_begin,
-                                                            int k0, int whole, int blocked, R tiny, int *tiny_count) {
+                                                            int k0, int whole, int blocked, R tiny, int *tiny_count,
+                                                            OpDev o, const int32_t *__restrict__ asm_vars,
+                                                            const int32_t *__restrict__ nbr_loc,
+                                                            const unsigned long long *maxdiag) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *D = reinterpret_cast<T *>(smem_raw);
     const FrontD f = fr[f_begin + blockIdx.x];
@@ -316,14 +349,21 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     const int64_t ld = f.ld;
     const int S = SC > 0 ? SC : (n + 15) / 16 * 16, LD = S + 1, NBLK = S / 16;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int c = warp; c < S; c += kDenseThreads / 32)
-        for (int r = lane; r < S; r += 32) {
-            if (r < n && c < n)
-                cp_async_elem(D + r + c * LD, G + r + (int64_t)c * ld);
-            else
-                D[r + c * LD] = (r == c) ? cone<T>() : czero<T>();
-        }
-    cp_async_wait_all();
+    if (ASM) {
+        for (int c = warp; c < S; c += kDenseThreads / 32)
+            for (int r = lane; r < S; r += 32) D[r + c * LD] = (r == c && r >= n) ? cone<T>() : czero<T>();
+        __syncthreads();
+        for (int k = tid; k < P; k += kDenseThreads) assemble_pivot(o, asm_vars[f.voff + k], k, P, nbr_loc, maxdiag, D, LD);
+    } else {
+        for (int c = warp; c < S; c += kDenseThreads / 32)
+            for (int r = lane; r < S; r += 32) {
+                if (r < n && c < n)
+                    cp_async_elem(D + r + c * LD, G + r + (int64_t)c * ld);
+                else
+                    D[r + c * LD] = (r == c) ? cone<T>() : czero<T>();
+            }
+        cp_async_wait_all();
+    }
     __syncthreads();
 
     const int tx = tid & 15, ty = tid >> 4;
@@ -480,19 +520,37 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
 // Launch k_dense_lu for blocks padded to S.  The 64-wide panel blocks and
 // the leaves' 80-row fronts have their own builds (about 10% faster there;
 // larger fixed sizes ran slower than the generic build).
+struct LeafAsm {
+    OpDev o{};
+    const int32_t *vars = nullptr, *nbr_loc = nullptr;
+    const unsigned long long *maxdiag = nullptr;
+};
+
 template <typename T, typename R>
 void dense_lu_launch(int nfl, int S, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0, int whole,
-                     int blocked, R tiny, int *tiny_count) {
+                     int blocked, R tiny, int *tiny_count, const LeafAsm &la = LeafAsm()) {
     const size_t smem = dense_lu_smem<T>(S);
+    if (la.vars) {
+        if (S == 80)
+            k_dense_lu<T, R, 80, true><<<nfl, kDenseThreads, smem, st>>>(
+                fr, pool, fb, k0, whole, blocked, tiny, tiny_count, la.o, la.vars, la.nbr_loc, la.maxdiag);
+        else
+            k_dense_lu<T, R, 0, true><<<nfl, kDenseThreads, smem, st>>>(
+                fr, pool, fb, k0, whole, blocked, tiny, tiny_count, la.o, la.vars, la.nbr_loc, la.maxdiag);
+        return;
+    }
     switch (S) {
     case 64:
-        k_dense_lu<T, R, 64><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
+        k_dense_lu<T, R, 64, false><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny,
+                                                                      tiny_count, la.o, nullptr, nullptr, nullptr);
         break;
     case 80:
-        k_dense_lu<T, R, 80><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
+        k_dense_lu<T, R, 80, false><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny,
+                                                                      tiny_count, la.o, nullptr, nullptr, nullptr);
         break;
     default:
-        k_dense_lu<T, R, 0><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny, tiny_count);
+        k_dense_lu<T, R, 0, false><<<nfl, kDenseThreads, smem, st>>>(fr, pool, fb, k0, whole, blocked, tiny,
+                                                                     tiny_count, la.o, nullptr, nullptr, nullptr);
     }
 }
 
@@ -1577,14 +1635,20 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
 template <typename T, typename R>
 int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
-    CUDA_TRY(cudaMemsetAsync(fac->d_pool, 0, (size_t)S.pool_entries * sizeof(T), st));
+    // the leaves (level 0), when factored whole, assemble their fronts in
+    // the LU kernel: their part of the pool is neither cleared nor written
+    // by the assembly kernel
+    const bool leaf_asm = S.nlev > 1 && dense_front_fits<T>(fac, S.lev_max_p[0], S.lev_max_m[0]);
+    const int f_skip = leaf_asm ? S.level_ptr[1] : 0;
+    const int64_t pool_skip = leaf_asm ? S.pool_off[S.level_ptr[1]] : 0;
+    CUDA_TRY(cudaMemsetAsync((T *)fac->d_pool + pool_skip, 0, (size_t)(S.pool_entries - pool_skip) * sizeof(T), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_tiny, 0, sizeof(int), st));
     if (fac->d_tcerr) CUDA_TRY(cudaMemsetAsync(fac->d_tcerr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_maxdiag, 0, sizeof(unsigned long long), st));
     prof_begin(PROF_ASSEMBLE, st);
     k_maxdiag<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_maxdiag);
     k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc,
-                                                       fac->d_nbr, fac->d_maxdiag, (T *)fac->d_pool);
+                                                       fac->d_nbr, fac->d_maxdiag, (T *)fac->d_pool, f_skip);
     prof_end(PROF_ASSEMBLE, st, 2);
     // Default static-pivot thresholds (relative to max|diag A|): sqrt(eps)
     // for complex128; 1e-5 for complex64, the value that minimised the
@@ -1621,8 +1685,15 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             // levels solved one warp per front keep the blocked pivot-block format
             const int blocked = maxm <= kWarpMaxM ? 1 : 0;
             fac->blocked_level[L] = (char)blocked;
+            LeafAsm la;
+            if (L == 0 && leaf_asm) {
+                la.o = o;
+                la.vars = fac->d_vars;
+                la.nbr_loc = fac->d_nbr;
+                la.maxdiag = fac->d_maxdiag;
+            }
             dense_lu_launch<T, R>(nfl, (maxm + 15) / 16 * 16, st, fac->d_fronts, pool, fb, 0, 1, blocked, tiny,
-                                  fac->d_tiny);
+                                  fac->d_tiny, la);
             prof_end(PROF_LU_DIAG, st, 1);
             continue;
         }
@@ -2046,11 +2117,15 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
 
 template <typename T, typename R>
 int set_smem_attrs() {
-    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
-    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
-    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 80>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 80, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDenseSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDenseSmemMax));
+    CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 80, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
 
     const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
