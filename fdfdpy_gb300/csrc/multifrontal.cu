@@ -108,13 +108,13 @@ __global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
                                   const int32_t *__restrict__ var_front,
                                   const int32_t *__restrict__ var_loc,
                                   const int32_t *__restrict__ nbr_loc,
-                                  const unsigned long long *maxdiag, T *pool, int f_skip) {
+                                  const unsigned long long *maxdiag, T *pool, int f_lo, int f_hi) {
     const int64_t n = (int64_t)o.Nx * o.Ny;
     const double sigma = 1.0 / __longlong_as_double((long long)*maxdiag);
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
          s += (int64_t)gridDim.x * blockDim.x) {
-        // fronts below f_skip (the leaves) are assembled by their LU kernel
-        if (var_front[s] < f_skip) continue;
+        // only the variables of fronts [f_lo, f_hi)
+        if (var_front[s] < f_lo || var_front[s] >= f_hi) continue;
         const int i = (int)(s / o.Ny), j = (int)(s % o.Ny);
         const FrontD f = fr[var_front[s]];
         T *F = pool + f.f_off;
@@ -142,31 +142,63 @@ __global__ void k_assemble_fronts(OpDev o, const FrontD *__restrict__ fr,
     }
 }
 
-// Extend-add: the parent pulls child `slot`'s update matrix.  A CTA takes
-// `cb` consecutive columns of the child's update block and spreads all of
-// their entries over its threads (rows fastest), so a small update block
-// (28 x 28 at the leaves) still keeps every thread busy and every thread
-// has several independent load-add-store chains.
+// Extend-add by the parent, written once: every entry (a, b) of the
+// parent's m x m block becomes the sum of the children's update-block
+// entries that map onto it (inv_s[a] = child s's update-block row of parent
+// row a, or -1), zero where none does, so the pool needs no clearing.  A
+// CTA takes cb consecutive columns, rows fastest.  The operator's entries
+// are added afterwards (k_assemble_level).
 template <typename T>
-__global__ void k_extend_add(const FrontD *__restrict__ fr, const int32_t *__restrict__ relmap,
-                             T *pool, int f_begin, int slot, int cb) {
+__global__ void k_extend_pull(const FrontD *__restrict__ fr, const int32_t *__restrict__ inv0,
+                              const int32_t *__restrict__ inv1, T *pool, int f_begin, int cb) {
     const FrontD f = fr[f_begin + blockIdx.x];
-    const int c = slot ? f.c1 : f.c0;
-    if (c < 0) return;
-    const FrontD ch = fr[c];
-    const int mu = ch.m - ch.p;
     const int b0 = blockIdx.y * cb;
-    if (b0 >= mu) return;
-    const int32_t *rm = relmap + ch.voff + ch.p;
-    const T *U = pool + ch.f_off + (int64_t)ch.p * ch.ld + ch.p;
-    T *P = pool + f.f_off;
-    const int64_t ldc = ch.ld, ldp = f.ld;
-    const int cols = min(cb, mu - b0);
-    const int total = cols * mu;
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        const int bb = idx / mu, a = idx - bb * mu, b = b0 + bb;
-        T &dst = P[rm[a] + (int64_t)rm[b] * ldp];
-        dst = cadd(dst, U[a + (int64_t)b * ldc]);
+    if (b0 >= f.m) return;
+    const int cols = min(cb, f.m - b0), m = f.m;
+    const T *U0 = nullptr, *U1 = nullptr;
+    int64_t ld0 = 0, ld1 = 0;
+    if (f.c0 >= 0) {
+        const FrontD c = fr[f.c0];
+        U0 = pool + c.f_off + (int64_t)c.p * c.ld + c.p;
+        ld0 = c.ld;
+    }
+    if (f.c1 >= 0) {
+        const FrontD c = fr[f.c1];
+        U1 = pool + c.f_off + (int64_t)c.p * c.ld + c.p;
+        ld1 = c.ld;
+    }
+    const int32_t *i0 = inv0 + f.voff, *i1 = inv1 + f.voff;
+    T *F = pool + f.f_off;
+    const int64_t ld = f.ld;
+    for (int idx = threadIdx.x; idx < cols * m; idx += blockDim.x) {
+        const int bb = idx / m, a = idx - bb * m, b = b0 + bb;
+        T v = czero<T>();
+        if (U0) {
+            const int ia = i0[a], ib = i0[b];
+            if (ia >= 0 && ib >= 0) v = U0[ia + (int64_t)ib * ld0];
+        }
+        if (U1) {
+            const int ia = i1[a], ib = i1[b];
+            if (ia >= 0 && ib >= 0) v = cadd(v, U1[ia + (int64_t)ib * ld1]);
+        }
+        F[a + (int64_t)b * ld] = v;
+    }
+}
+
+// Row k and the boundary entries of column k of every pivot of one level
+// (piv: the level's pivot variables, front by front), added to the pulled
+// blocks; one thread per pivot.
+template <typename T>
+__device__ __forceinline__ void assemble_pivot(const OpDev &o, int sv, int k, int P, const int32_t *__restrict__ nbr_loc,
+                                               const unsigned long long *maxdiag, T *D, int LD);
+template <typename T>
+__global__ void k_assemble_level(OpDev o, const FrontD *__restrict__ fr, const int32_t *__restrict__ piv, int count,
+                                 const int32_t *__restrict__ var_front, const int32_t *__restrict__ var_loc,
+                                 const int32_t *__restrict__ nbr_loc, const unsigned long long *maxdiag, T *pool) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+        const int sv = piv[idx];
+        const FrontD f = fr[var_front[sv]];
+        assemble_pivot(o, sv, var_loc[sv], f.p, nbr_loc, maxdiag, pool + f.f_off, (int)f.ld);
     }
 }
 
@@ -1519,6 +1551,9 @@ struct fdfd_factor {
     int64_t n = 0;
     // device arrays
     FrontD *d_fronts = nullptr;
+    int32_t *d_inv = nullptr;  // per front row: child 0's, then child 1's update-block row (2 x sum_m), or -1
+    int32_t *d_piv = nullptr;  // pivot variables front by front (n); level L's are [piv_off[L], piv_off[L + 1])
+    std::vector<int64_t> piv_off;
     int32_t *d_vars = nullptr, *d_relmap = nullptr, *d_nbr = nullptr, *d_vfront = nullptr,
             *d_vloc = nullptr;
     void *d_pool = nullptr, *d_W = nullptr, *d_Y = nullptr;
@@ -1635,21 +1670,23 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
 template <typename T, typename R>
 int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
-    // the leaves (level 0), when factored whole, assemble their fronts in
-    // the LU kernel: their part of the pool is neither cleared nor written
-    // by the assembly kernel
-    const bool leaf_asm = S.nlev > 1 && dense_front_fits<T>(fac, S.lev_max_p[0], S.lev_max_m[0]);
-    const int f_skip = leaf_asm ? S.level_ptr[1] : 0;
-    const int64_t pool_skip = leaf_asm ? S.pool_off[S.level_ptr[1]] : 0;
-    CUDA_TRY(cudaMemsetAsync((T *)fac->d_pool + pool_skip, 0, (size_t)(S.pool_entries - pool_skip) * sizeof(T), st));
+    // Every front above the leaves is written whole by the parent-side
+    // extend-add and then takes its operator entries; the leaves (level 0),
+    // when factored whole, assemble their fronts in the LU kernel, else
+    // their part of the pool is cleared and assembled here.  No other part
+    // of the pool is cleared.
+    const bool leaf_asm = dense_front_fits<T>(fac, S.lev_max_p[0], S.lev_max_m[0]);
+    const int64_t leaf_entries = S.nlev > 1 ? S.pool_off[S.level_ptr[1]] : S.pool_entries;
+    if (!leaf_asm) CUDA_TRY(cudaMemsetAsync(fac->d_pool, 0, (size_t)leaf_entries * sizeof(T), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_tiny, 0, sizeof(int), st));
     if (fac->d_tcerr) CUDA_TRY(cudaMemsetAsync(fac->d_tcerr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_maxdiag, 0, sizeof(unsigned long long), st));
     prof_begin(PROF_ASSEMBLE, st);
     k_maxdiag<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_maxdiag);
-    k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc,
-                                                       fac->d_nbr, fac->d_maxdiag, (T *)fac->d_pool, f_skip);
-    prof_end(PROF_ASSEMBLE, st, 2);
+    if (!leaf_asm)
+        k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc, fac->d_nbr,
+                                                           fac->d_maxdiag, (T *)fac->d_pool, 0, S.level_ptr[1]);
+    prof_end(PROF_ASSEMBLE, st, leaf_asm ? 1 : 2);
     // Default static-pivot thresholds (relative to max|diag A|): sqrt(eps)
     // for complex128; 1e-5 for complex64, the value that minimised the
     // refinement steps of the 2048^2 Hz workload (sqrt(eps_f32) = 3.4e-4
@@ -1662,21 +1699,19 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     for (int L = 0; L < S.nlev; ++L) {
         const int fb = S.level_ptr[L], nfl = S.level_ptr[L + 1] - fb;
         if (L > 0) {
-            int maxmu = 0;
-            for (int f = fb; f < fb + nfl; ++f) {
-                const int cs[2] = {S.child0[f], S.child1[f]};
-                for (int c : cs)
-                    if (c >= 0) maxmu = std::max(maxmu, S.m[c] - S.p[c]);
-            }
-            if (maxmu > 0) {
-                // about 2048 entries per CTA; at most (1 << 30) / maxmu columns so idx fits in int
-                const int cb = std::max(1, 2048 / maxmu);
-                dim3 g(nfl, (maxmu + cb - 1) / cb);
-                prof_begin(PROF_EXTEND_ADD, st);
-                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 0, cb);
-                k_extend_add<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_relmap, pool, fb, 1, cb);
-                prof_end(PROF_EXTEND_ADD, st, 2);
-            }
+            // about 2048 entries per CTA; at most (1 << 30) / maxm columns so idx fits in int
+            const int maxm_l = S.lev_max_m[L];
+            const int cb = std::max(1, 2048 / maxm_l);
+            dim3 g(nfl, (maxm_l + cb - 1) / cb);
+            prof_begin(PROF_EXTEND_ADD, st);
+            k_extend_pull<T><<<g, 256, 0, st>>>(fac->d_fronts, fac->d_inv, fac->d_inv + S.sum_m, pool, fb, cb);
+            prof_end(PROF_EXTEND_ADD, st, 1);
+            prof_begin(PROF_ASSEMBLE, st);
+            const int np = (int)(fac->piv_off[L + 1] - fac->piv_off[L]);
+            k_assemble_level<T><<<std::max(1, (np + 255) / 256), 256, 0, st>>>(
+                o, fac->d_fronts, fac->d_piv + fac->piv_off[L], np, fac->d_vfront, fac->d_vloc, fac->d_nbr,
+                fac->d_maxdiag, pool);
+            prof_end(PROF_ASSEMBLE, st, 1);
         }
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         if (dense_front_fits<T>(fac, maxp, maxm)) {
@@ -2334,7 +2369,7 @@ int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, in
 
 void free_factor(fdfd_factor *f) {
     if (!f) return;
-    void *ptrs[] = {f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
+    void *ptrs[] = {f->d_inv, f->d_piv, f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
                     f->d_norm, f->d_sin, f->d_sout, f->d_unit, f->d_maxdiag, f->d_tiny,
                     f->d_tcf, f->d_scratch, f->d_tcerr, f->d_bwd_off, f->d_bwd_scratch,
@@ -2478,7 +2513,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += 2 * S.sum_m * max_nrhs * elem;                  // W, Y
     b += 3 * n * max_nrhs * 16;                          // r, d, tmp
     b += (int64_t)S.nf * sizeof(FrontD);
-    b += 2 * S.sum_m * 4 + 6 * n * 4;                    // vars, relmap, nbr, var maps
+    b += 4 * S.sum_m * 4 + 7 * n * 4;                    // vars, relmap, inverse maps, nbr, var maps, pivots
     b += (int64_t)(S.Nx + S.Ny) * 16;
     b += 5 * n * 16;                                     // operator coefficients
     b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
@@ -2567,6 +2602,7 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
     const int64_t n = f->n;
     bool ok = alloc((void **)&f->d_fronts, S.nf * sizeof(FrontD)) &&
               alloc((void **)&f->d_vars, S.sum_m * 4) && alloc((void **)&f->d_relmap, S.sum_m * 4) &&
+              alloc((void **)&f->d_inv, 2 * S.sum_m * 4) && alloc((void **)&f->d_piv, n * 4) &&
               alloc((void **)&f->d_nbr, 4 * n * 4) && alloc((void **)&f->d_vfront, n * 4) &&
               alloc((void **)&f->d_vloc, n * 4) && alloc(&f->d_pool, S.pool_entries * f->elem) &&
               alloc(&f->d_W, S.sum_m * max_nrhs * f->elem) &&
@@ -2591,6 +2627,28 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
     if (e == cudaSuccess) e = cudaMemcpy(f->d_fronts, fd.data(), S.nf * sizeof(FrontD), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(f->d_vars, S.vars.data(), S.sum_m * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(f->d_relmap, S.relmap.data(), S.sum_m * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        // inverse of the children's row maps, for the parent-side extend-add
+        std::vector<int32_t> inv((size_t)2 * S.sum_m, -1);
+        for (int32_t c = 0; c < S.nf; ++c) {
+            const int32_t par = S.parent[c];
+            if (par < 0) continue;
+            const int64_t base = (S.child0[par] == c ? 0 : S.sum_m) + S.vars_off[par];
+            for (int32_t k = S.p[c]; k < S.m[c]; ++k) inv[base + S.relmap[S.vars_off[c] + k]] = k - S.p[c];
+        }
+        e = cudaMemcpy(f->d_inv, inv.data(), inv.size() * 4, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        std::vector<int32_t> piv;
+        piv.reserve(n);
+        f->piv_off.assign(S.nlev + 1, 0);
+        for (int L = 0; L < S.nlev; ++L) {
+            for (int32_t fr = S.level_ptr[L]; fr < S.level_ptr[L + 1]; ++fr)
+                for (int32_t k = 0; k < S.p[fr]; ++k) piv.push_back(S.vars[S.vars_off[fr] + k]);
+            f->piv_off[L + 1] = (int64_t)piv.size();
+        }
+        e = cudaMemcpy(f->d_piv, piv.data(), piv.size() * 4, cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemcpy(f->d_nbr, S.nbr_loc.data(), 4 * n * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(f->d_vfront, S.var_front.data(), n * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(f->d_vloc, S.var_loc.data(), n * 4, cudaMemcpyHostToDevice);
