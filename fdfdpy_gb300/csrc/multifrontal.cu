@@ -595,7 +595,8 @@ enum GemmMode { SCHUR = 0, TRSM_L = 1, TRSM_U = 2 };
 //   TRSM_U: F[k0:k0+w, t0:] = inv(L_kk) F[k0:k0+w, t0:]      (in place)
 // In the in-place modes a CTA owns complete rows (TRSM_L) or columns
 // (TRSM_U) of its output and reads all of them before writing.
-template <typename T, typename R, int MODE>
+// QA x QB 16-row / 16-column groups per thread: the tile is (16 QA) x (16 QB).
+template <typename T, typename R, int MODE, int QA = 4, int QB = 4>
 __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, int ytile,
                                           int ztile, T (*As)[BM + 1], T (*Bs)[BN + 1], uint8_t *bpack = nullptr) {
     const FrontD f = fr[f_begin + blockIdx.x];
@@ -603,30 +604,31 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
     if (w <= 0) return;
     const int t0 = k0 + w;
     const int m = f.m;
+    constexpr int TM = 16 * QA, TN = 16 * QB;
     int rbase, cbase, rend, cend;
     if (MODE == SCHUR) {
-        rbase = t0 + ytile * BM; cbase = t0 + ztile * BN; rend = m; cend = m;
+        rbase = t0 + ytile * TM; cbase = t0 + ztile * TN; rend = m; cend = m;
     } else if (MODE == TRSM_L) {
-        rbase = t0 + ytile * BM; cbase = k0; rend = m; cend = t0;
+        rbase = t0 + ytile * TM; cbase = k0; rend = m; cend = t0;
     } else {
-        rbase = k0; cbase = t0 + ztile * BN; rend = t0; cend = m;
+        rbase = k0; cbase = t0 + ztile * TN; rend = t0; cend = m;
     }
     if (rbase >= rend || cbase >= cend) return;
     T *F = pool + f.f_off;
     const int64_t ld = f.ld;
     const int tid = threadIdx.x;
     const int tx = tid % 16, ty = tid / 16;
-    T acc[4][4];
+    T acc[QA][QB];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < QA; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = czero<T>();
+        for (int b = 0; b < QB; ++b) acc[a][b] = czero<T>();
 
     // The A and B elements of K chunk kc + BK load into registers while
     // chunk kc is multiplied out of shared memory.
     auto load_a = [&](int kc, int q) -> T {
         const int idx = tid + 256 * q;
-        const int rr = idx % BM, kk = idx / BM;
+        const int rr = idx % TM, kk = idx / TM;
         const int r = rbase + rr, kg = kc + kk;
         T v = czero<T>();
         if (r < rend && kg < w) {
@@ -657,26 +659,28 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
         }
         return v;
     };
-    T pa[4], pb[4];
+    T pa[QA], pb[QB];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        pa[q] = load_a(0, q);
-        pb[q] = load_b(0, q);
-    }
+    for (int q = 0; q < QA; ++q) pa[q] = load_a(0, q);
+#pragma unroll
+    for (int q = 0; q < QB; ++q) pb[q] = load_b(0, q);
     for (int kc = 0; kc < w; kc += BK) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < QA; ++q) {
             const int idx = tid + 256 * q;
-            As[idx / BM][idx % BM] = pa[q];
+            As[idx / TM][idx % TM] = pa[q];
+        }
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int idx = tid + 256 * q;
             Bs[idx % BK][idx / BK] = pb[q];
         }
         __syncthreads();
         if (kc + BK < w) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                pa[q] = load_a(kc + BK, q);
-                pb[q] = load_b(kc + BK, q);
-            }
+            for (int q = 0; q < QA; ++q) pa[q] = load_a(kc + BK, q);
+#pragma unroll
+            for (int q = 0; q < QB; ++q) pb[q] = load_b(kc + BK, q);
         }
         // the triangular inverses are zero below (inv(U), TRSM_L) or above
         // (inv(L), TRSM_U) their diagonal: K chunk kc adds nothing to the
@@ -684,17 +688,16 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
         const int kcb = kc / 16;
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            T a[4], b[4];
+            T a[QA], b[QB];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                a[q] = As[kk][ty + 16 * q];
-                b[q] = Bs[kk][tx + 16 * q];
-            }
+            for (int q = 0; q < QA; ++q) a[q] = As[kk][ty + 16 * q];
 #pragma unroll
-            for (int qa = 0; qa < 4; ++qa) {
+            for (int q = 0; q < QB; ++q) b[q] = Bs[kk][tx + 16 * q];
+#pragma unroll
+            for (int qa = 0; qa < QA; ++qa) {
                 if (MODE == TRSM_U && qa < kcb) continue;
 #pragma unroll
-                for (int qb = 0; qb < 4; ++qb) {
+                for (int qb = 0; qb < QB; ++qb) {
                     if (MODE == TRSM_L && qb < kcb) continue;
                     cmac(acc[qa][qb], a[qa], b[qb]);
                 }
@@ -703,11 +706,11 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
         __syncthreads();
     }
 #pragma unroll
-    for (int qa = 0; qa < 4; ++qa) {
+    for (int qa = 0; qa < QA; ++qa) {
         const int r = rbase + ty + 16 * qa;
         if (r >= rend) continue;
 #pragma unroll
-        for (int qb = 0; qb < 4; ++qb) {
+        for (int qb = 0; qb < QB; ++qb) {
             const int c = cbase + tx + 16 * qb;
             if (c >= cend) continue;
             T &dst = F[r + (int64_t)c * ld];
@@ -721,10 +724,10 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
         if (bpack) {
             const int cts = (m - t0 + kTileNc - 1) / kTileNc;
 #pragma unroll
-            for (int qa = 0; qa < 4; ++qa) {
+            for (int qa = 0; qa < QA; ++qa) {
                 const int r = rbase + ty + 16 * qa, l = r - k0;
 #pragma unroll
-                for (int qb = 0; qb < 4; ++qb) {
+                for (int qb = 0; qb < QB; ++qb) {
                     const int c = cbase + tx + 16 * qb, cc = c - t0, ct = cc / kTileNc;
                     if (ct >= cts) continue;
                     const c64 v = (r < rend && c < cend) ? acc[qa][qb] : czero<c64>();
@@ -746,16 +749,33 @@ __global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ f
 // Both triangular updates of a panel step in one launch: blockIdx.z = 0
 // forms L (row tile blockIdx.y), blockIdx.z = 1 forms U (column tile
 // blockIdx.y) and, on tensor-core levels (tcf != NULL), its packed tiles.
-template <typename T, typename R>
+// HALF: 32-row (L) / 32-column (U) tiles, twice the CTAs, for levels with
+// few fronts whose triangular updates would not fill the GPU.
+template <typename T, typename R, bool HALF>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
                                                     const TcFront *__restrict__ tcf, uint8_t *scratch) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
     if (blockIdx.z == 0) {
-        gemm_tile<T, R, TRSM_L>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
+        gemm_tile<T, R, TRSM_L, HALF ? 2 : 4, 4>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
     } else {
         uint8_t *bpack = tcf ? scratch + tcf[f_begin + blockIdx.x].b_off : nullptr;
-        gemm_tile<T, R, TRSM_U>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
+        gemm_tile<T, R, TRSM_U, 4, HALF ? 2 : 4>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
+    }
+}
+
+// Both triangular updates of panel k0 for the fronts of a level (trail: an
+// upper bound of m - t0).  Half-height tiles while the level would launch
+// fewer than 1024 CTAs.
+template <typename T, typename R>
+void trsm_launch(int nfl, int trail, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0,
+                 const TcFront *tcf, uint8_t *scratch) {
+    const int tiles = (trail + BM - 1) / BM;
+    if (nfl * tiles * 2 < 1024) {
+        const int t2 = (trail + BM / 2 - 1) / (BM / 2);
+        k_trsm_panel<T, R, true><<<dim3(nfl, t2, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+    } else {
+        k_trsm_panel<T, R, false><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     }
 }
 
@@ -1639,10 +1659,8 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
     for (int k0 = 0; k0 < maxp; k0 += NB) {
         const int trail = maxm - k0 - 1;  // upper bound of m - t0
         if (trail <= 0) continue;
-        const int tiles = (trail + BM - 1) / BM;
         prof_begin(PROF_TRSM, st);
-        k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0, fac->d_tcf,
-                                                                fac->d_scratch);
+        trsm_launch<T, R>(nfl, trail, st, fac->d_fronts, pool, fb, k0, fac->d_tcf, fac->d_scratch);
         prof_end(PROF_TRSM, st, 1);
         prof_begin(PROF_SCHUR, st);
         int rc = FDFD_OK;
@@ -1746,9 +1764,8 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             if (trail <= 0) continue;
             const int tiles = (trail + BM - 1) / BM;
             prof_begin(PROF_TRSM, st);
-            k_trsm_panel<T, R><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fac->d_fronts, pool, fb, k0,
-                                                                    tc ? fac->d_tcf : nullptr,
-                                                                    tc ? fac->d_scratch : nullptr);
+            trsm_launch<T, R>(nfl, trail, st, fac->d_fronts, pool, fb, k0, tc ? fac->d_tcf : nullptr,
+                              tc ? fac->d_scratch : nullptr);
             prof_end(PROF_TRSM, st, 1);
             if (tc) {
                 prof_begin(PROF_SCHUR, st);
