@@ -47,6 +47,20 @@ def as_c128(x, shape=None) -> torch.Tensor:
     return t if shape is None else t.reshape(shape)
 
 
+def to_host(*ts):
+    """Device tensors -> numpy arrays through page-locked buffers from
+    torch's caching host allocator (the copies run at link speed, with no
+    staging copy on the host; a buffer is reused once the caller has dropped
+    an earlier result).  One synchronisation for all of them."""
+    hs = []
+    for t in ts:
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t, non_blocking=True)
+        hs.append(h)
+    torch.cuda.current_stream().synchronize()
+    return [h.numpy() for h in hs]
+
+
 def as_f64(x) -> torch.Tensor:
     dev = device()
     if isinstance(x, torch.Tensor):

@@ -176,10 +176,12 @@ class Simulation:
         else:
             eps_dev = self._op.eps if self.pol == 'Hz' else None
         f1, f2 = self._op.fields(X, averaging=averaging, eps=eps_dev)
-        F1 = f1.cpu().numpy().reshape((Nx, Ny))
-        F2 = f2.cpu().numpy().reshape((Nx, Ny))
-        # an all-zero source gives float zeros for the primary field (linalg.py:128-129)
-        F3 = np.zeros((Nx, Ny)) if zero_src else X.cpu().numpy().reshape((Nx, Ny))
+        if zero_src:
+            # an all-zero source gives float zeros for the primary field (linalg.py:128-129)
+            F1, F2 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2))
+            F3 = np.zeros((Nx, Ny))
+        else:
+            F1, F2, F3 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2, X))
         if timing:
             print('Linear system solve took {:.2f} seconds'.format(time() - t))
         if self.pol == 'Hz':
