@@ -338,12 +338,21 @@ __global__ void __maxnreg__(128)
         for (int j = 0; j < J; ++j) {
             const int sidx = j & 1;
             const int colbase = t0 + (ct0 + j) * kTileNc + kHalf * h;
-            // the next tile's C entries load while this tile's MMAs finish
+            // the next tile's C entries load while this tile's MMAs finish,
+            // and the one after that is prefetched into L2 (no registers)
             if (j + 1 < J) {
 #pragma unroll
                 for (int q = 0; q < kHalf; ++q) {
                     const int col = colbase + kTileNc + q;
                     nv[q] = (live && col < f.m) ? F[row + (int64_t)col * ld] : czero<c64>();
+                }
+            }
+            if (j + 2 < J && live) {
+#pragma unroll
+                for (int q = 0; q < kHalf; ++q) {
+                    const int col = colbase + 2 * kTileNc + q;
+                    if (col < f.m)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(F + row + (int64_t)col * ld) : "memory");
                 }
             }
             const bool got = mbar_wait_bounded(&bar_mma[sidx], (j >> 1) & 1, kWaitLimit);
