@@ -1602,7 +1602,7 @@ struct fdfd_factor {
     int64_t *d_bwd_off = nullptr;
     void *d_bwd_scratch = nullptr;
     double pivot_tol = -1.0;  // relative static-pivot threshold (<0: default)
-    int fused_max_m = -1;     // largest front factored in one launch (<0: shared-memory limit)
+    int fused_max_m = -1;     // largest front factored in one launch (<0: the default of dense_front_fits)
     // coefficients of the factored operator (see k_coef) and the operator
     // description they belong to
     double2 *d_coef = nullptr;
@@ -1633,12 +1633,22 @@ namespace {
 
 
 // A level is factored front-by-front in one launch when all its fronts have
-// at most 64 pivots and the largest front fits in shared memory (and under
-// the caller's size limit, if set).
+// at most 64 pivots, the largest front fits in shared memory and is at most
+// the size limit.  Default: any size for levels of fewer than
+// kFusedManyFronts fronts (one launch instead of three per level matters
+// for small problems), kWarpMaxM rows for wider levels (larger fronts
+// leave one 256-thread CTA an SM and ran faster through the per-panel
+// kernels: 2048^2 Hz, 4096 fronts of 155 rows, 54.9 -> 54.2 ms a
+// factorization).  Else the caller's limit.
+constexpr int kFusedManyFronts = 2048;
 template <typename T>
-bool dense_front_fits(const fdfd_factor *fac, int maxp, int maxm) {
+bool dense_front_fits(const fdfd_factor *fac, int maxp, int maxm, int nfl) {
     if (maxp > kDenseMaxPiv || maxm <= 0) return false;
-    if (fac->fused_max_m >= 0 && maxm > fac->fused_max_m) return false;
+    if (fac->fused_max_m >= 0) {
+        if (maxm > fac->fused_max_m) return false;
+    } else if (nfl >= kFusedManyFronts && maxm > kWarpMaxM) {
+        return false;
+    }
     return dense_lu_smem<T>(maxm) <= kDenseSmemMax;
 }
 
@@ -1693,7 +1703,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     // when factored whole, assemble their fronts in the LU kernel, else
     // their part of the pool is cleared and assembled here.  No other part
     // of the pool is cleared.
-    const bool leaf_asm = dense_front_fits<T>(fac, S.lev_max_p[0], S.lev_max_m[0]);
+    const bool leaf_asm = dense_front_fits<T>(fac, S.lev_max_p[0], S.lev_max_m[0], S.level_ptr[1] - S.level_ptr[0]);
     const int64_t leaf_entries = S.nlev > 1 ? S.pool_off[S.level_ptr[1]] : S.pool_entries;
     if (!leaf_asm) CUDA_TRY(cudaMemsetAsync(fac->d_pool, 0, (size_t)leaf_entries * sizeof(T), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_tiny, 0, sizeof(int), st));
@@ -1732,7 +1742,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             prof_end(PROF_ASSEMBLE, st, 1);
         }
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
-        if (dense_front_fits<T>(fac, maxp, maxm)) {
+        if (dense_front_fits<T>(fac, maxp, maxm, nfl)) {
             // every front of the level in one launch: LU, L21, U12 and the update matrix
             prof_begin(PROF_LU_DIAG, st);
             // levels solved one warp per front keep the blocked pivot-block format

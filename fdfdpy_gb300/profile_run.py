@@ -36,7 +36,7 @@ def main(argv=None):
     ap.add_argument("--nrhs", type=int, default=1)
     ap.add_argument("--leaf", type=int, default=None, help="leaf area of the nested dissection")
     ap.add_argument("--fused-max-m", type=int, default=None,
-                    help="largest front factored in one launch per level (-1: shared-memory limit, 0: never)")
+                    help="largest front factored in one launch per level (-1: the default; 0: never)")
     ap.add_argument("--repeat", type=int, default=1, help="timed factorizations outside the ranges")
     args = ap.parse_args(argv)
     N = args.size

@@ -250,10 +250,11 @@ int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
 int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol);
 /* Largest front size m that is factored by one launch per level (all of
  * a level's fronts must have at most 64 pivots; the dense front is held in
- * shared memory, which also bounds m).  -1 (default): as large as shared
- * memory allows; 0: never (every front goes through the per-panel
- * kernels).  Takes effect at the next fdfd_factor_numeric.  No
- * counterpart in fdfdpy.                                                 */
+ * shared memory, which also bounds m).  -1 (default): as large as
+ * shared memory allows on levels of fewer than 2048 fronts, 128 on wider
+ * levels; 0: never (every front goes through the per-panel kernels).
+ * Takes effect at the next fdfd_factor_numeric.  No counterpart in
+ * fdfdpy.                                                                */
 int fdfd_factor_set_fused_limit(fdfd_factor *fac, int32_t max_m);
 /* One right-hand side by restarted GMRES(restart) in FP64, right-
  * preconditioned by the factor; stops at ||b - A x|| <= tol ||b|| or after
