@@ -95,11 +95,14 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def schur_work(sym, elem=8, nb=64):
+def schur_work(sym, elem=8, nb=64, tc_only=True):
     """Algorithmic work of the Schur-complement updates of one factor run by
-    the Schur kernels (levels not factored whole in shared memory): real
-    flops 8 w t^2 and bytes (C read and written once, L and U panels read
-    once) elem * (2 t^2 + 2 t w) per front and panel, t = m - k0 - w."""
+    the Schur kernels: real flops 8 w t^2 and bytes (C read and written
+    once, L and U panels read once) elem * (2 t^2 + 2 t w) per front and
+    panel, t = m - k0 - w.  Levels factored whole in shared memory are left
+    out (the engine's default rule: at most 64 pivots, the padded front in
+    220 KB, and at most 128 rows on levels of 2048 or more fronts); with
+    tc_only, so are the levels below 192 rows (SIMT form)."""
     info = sym.info
     p = sym.export(0, info.n_fronts).astype(np.int64)
     m = sym.export(1, info.n_fronts).astype(np.int64)
@@ -107,8 +110,11 @@ def schur_work(sym, elem=8, nb=64):
     keep = np.ones(info.n_fronts, dtype=bool)
     for L in range(info.n_levels):
         sl = slice(lp[L], lp[L + 1])
-        S = (int(m[sl].max()) + 15) // 16 * 16
-        if int(p[sl].max()) <= nb and S * (S + 1) * elem <= 220 * 1024:  # whole-front kernel
+        mmax, nfl = int(m[sl].max()), int(lp[L + 1] - lp[L])
+        S = (mmax + 15) // 16 * 16
+        whole = (int(p[sl].max()) <= nb and S * (S + 1) * elem <= 220 * 1024
+                 and (nfl < 2048 or mmax <= 128))
+        if whole or (tc_only and mmax < 192):
             keep[sl] = False
     p, m = p[keep], m[keep]
     flops = byts = 0.0
@@ -390,8 +396,9 @@ def main():
         return
     value = world * 1e3 / ms
     prof = res["profile"]
-    schur_ms, schur_n = prof["schur"]
-    fl, by = schur_work(res["sym"], 16 if args.precision == "c128" else 8)
+    tc = args.precision == "c64tc"
+    schur_ms, schur_n = prof["schur"] if tc else prof["schur_simt"]
+    fl, by = schur_work(res["sym"], 16 if args.precision == "c128" else 8, tc_only=tc)
     achieved = by / (schur_ms * 1e-3) / 1e9 if schur_ms > 0 else None
     peaks = {}
     try:
@@ -422,8 +429,8 @@ def main():
         "mixed": {"rel_residual": res["stats64"]["rel_residual"], "refine_iters": res["stats64"]["refine_iters"],
                   "tiny_pivots": res["stats64"]["tiny_pivots"],
                   "field_err_vs_c128": res.get("field_err_vs_c128")},
-        "roofline": {"kernel": ("Schur-complement update: k_schur_tc (tcgen05 kind::tf32, 3xTF32) on fronts "
-                               "with m >= 192, k_schur_simt below" if args.precision == "c64tc"
+        "roofline": {"kernel": ("Schur-complement update k_schur_tc (tcgen05 kind::tf32, 3xTF32), the levels "
+                               "of fronts with m >= 192" if tc
                                else "Schur-complement update: k_schur_simt (SIMT complex)"),
                      "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

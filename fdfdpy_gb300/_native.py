@@ -97,7 +97,8 @@ SIGNATURES = {
     "fdfd_profile_read": (C.c_int, [I32, P, P]),
 }
 
-PROFILE_CLASSES = ("assemble", "extend_add", "lu_diag", "trsm", "schur", "solve_fwd", "solve_bwd", "other")
+PROFILE_CLASSES = ("assemble", "extend_add", "lu_diag", "trsm", "schur", "solve_fwd", "solve_bwd", "other",
+                   "schur_simt")
 
 
 def profile_read():

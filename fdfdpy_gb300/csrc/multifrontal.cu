@@ -1784,9 +1784,9 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
                 if (rc) return rc;
                 prof_end(PROF_SCHUR, st, 1);
             } else {
-                prof_begin(PROF_SCHUR, st);
+                prof_begin(PROF_SCHUR_SIMT, st);
                 k_schur_simt<T, R><<<dim3(nfl, tiles, tiles), 256, 0, st>>>(fac->d_fronts, pool, fb, k0);
-                prof_end(PROF_SCHUR, st, 1);
+                prof_end(PROF_SCHUR_SIMT, st, 1);
             }
         }
     }

@@ -16,7 +16,8 @@ enum ProfClass {
     PROF_SOLVE_FWD = 5,
     PROF_SOLVE_BWD = 6,
     PROF_OTHER = 7,
-    PROF_NCLASS = 8
+    PROF_SCHUR_SIMT = 8,
+    PROF_NCLASS = 9
 };
 
 void prof_begin(int cls, cudaStream_t st);

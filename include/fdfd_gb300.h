@@ -271,13 +271,15 @@ void fdfd_factor_destroy(fdfd_factor *fac);
 /* ---- profiling -----------------------------------------------------------
  * Launch counters per kernel class are always kept; CUDA-event timing of
  * each class is recorded while enabled.  Classes: 0 front assembly,
- * 1 extend-add, 2 diagonal-block LU, 3 panel TRSM, 4 Schur GEMM,
- * 5 forward solve, 6 backward solve, 7 residual / norms / scaling.
+ * 1 extend-add, 2 diagonal-block LU, 3 panel TRSM, 4 Schur GEMM on the
+ * tensor cores, 5 forward solve, 6 backward solve, 7 residual / norms /
+ * scaling, 8 Schur GEMM in SIMT form (fronts below 192 rows, complex128,
+ * complex64 without tensor cores).
  * Replaces the `timing=` prints of the reference (fdfdpy/linalg.py:131-147).
  * Not thread-safe: profile one stream at a time.                         */
 int fdfd_profile_enable(int32_t on);
 int fdfd_profile_reset(void);
-/* Synchronises on the recorded events; writes nclass (<= 8) entries.     */
+/* Synchronises on the recorded events; writes nclass (<= 9) entries.     */
 int fdfd_profile_read(int32_t nclass, double *ms, int64_t *launches);
 
 #ifdef __cplusplus
