@@ -74,3 +74,17 @@ def test_cached_factor_is_reused_for_new_sources():
     s = srv.run([first, second], realtime=True)
     assert s["failed"] == 0 and s["cache_hits"] == 1 and second.cache_hit
     assert second.x.shape == (5, n) and second.rel_residual <= 1e-10
+
+
+def test_unconverged_request_is_solved_again_in_complex128():
+    """A request whose complex64 refinement stops short of the tolerance
+    (here: one refinement step against 1e-13) is solved again with a
+    complex128 factor, flagged, and meets the tolerance."""
+    from fdfdpy_gb300.serving import SolveServer
+    reqs = _requests()[:3]
+    srv = SolveServer(slots=2, precision="c64", tol=1e-13, max_iter=1)
+    s = srv.run(reqs, realtime=False)
+    assert s["failed"] == 0, [r.error for r in reqs if r.error]
+    assert s["c128_fallbacks"] == len(reqs)
+    for r in reqs:
+        assert r.fallback and r.rel_residual <= 1e-13, (r.rid, r.rel_residual)
