@@ -10,19 +10,24 @@
 //   * right of the diagonal blocks: U,
 //   * each nb x nb diagonal block: inv(L_kk) strictly below its diagonal
 //     and inv(U_kk) on and above it (both triangular inverses are used by
-//     the TRSM-as-GEMM updates and by the blocked triangular solves),
+//     the TRSM-as-GEMM updates and by the blocked triangular solves); the
+//     whole fronts of the levels solved one warp per front keep these
+//     inverses only inside 16 x 16 diagonal blocks (blocked format),
 //   * the trailing (m-p) x (m-p) block: the update (Schur complement)
-//     matrix that the parent pulls in by extend-add.
+//     matrix that the parent gathers by its extend-add.
 // The operator is factored scaled by sigma = 1/max|diag(A)| so that the
 // complex64 factor stays well inside float range (Hz entries reach 1e21).
 //
-// Pivoting is static: no row exchanges, and a pivot smaller than
-// sqrt(eps_T) (relative to the scaled operator) is replaced and counted;
-// the FP64 iterative refinement absorbs the perturbation.
+// Pivoting is static: no row exchanges, and a pivot below a threshold
+// relative to the scaled operator (1e-5 for complex64, sqrt(eps) for
+// complex128, or the caller's) is replaced and counted; the FP64
+// iterative refinement absorbs the perturbation.
 //
 // Parallel schedule: fronts are processed level by level (leaves first).
 // Each launch handles every front of a level: grid.x = front, grid.y/z =
-// tiles of that front.
+// tiles of that front.  Fronts above the leaves are written whole by the
+// parent-side extend-add (the pool is never cleared); the leaves assemble
+// their fronts inside their LU launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
