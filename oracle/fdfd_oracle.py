@@ -348,6 +348,28 @@ def solve_complex2real(A11, A12, b):
     return x[:n] + 1j * x[n:]
 
 
+def born_kerr_Ez(omega, xlen, ylen, eps_r, NPML, L0, src, chi, region, eps_scale=False, eps_max=None,
+                 conv_threshold=1e-10, max_num_iter=50):
+    """Born fixed point of born_solve (nonlinear_solvers.py:13-54) for one
+    Kerr term, Ez, from the linear solution: E <- (A + Anl(E))^-1 b with
+    Anl = diag(omega^2 eps0 L0 eps_nl) (simulation.py:57-68); returns
+    (Ez, conv list), Ez being the last iteration's solve."""
+    eps_r = np.asarray(eps_r, dtype=np.float64)
+    A = construct_A(omega, xlen, ylen, eps_r, NPML, 'Ez', L0)
+    b = (1j * omega * np.asarray(src)).reshape(-1).astype(np.complex128)
+    E = solve(A, b)
+    conv = []
+    for _ in range(max_num_iter):
+        eps_nl, _ = kerr_terms(E, eps_r.reshape(-1), chi, region.reshape(-1), eps_scale, eps_max)
+        En = solve(A + sp.diags(omega ** 2 * EPSILON_0 * L0 * eps_nl), b)
+        c = np.linalg.norm(En - E) / np.linalg.norm(En)
+        conv.append(c)
+        E = En
+        if c < conv_threshold:
+            break
+    return E, conv
+
+
 def newton_kerr_Ez(omega, xlen, ylen, eps_r, NPML, L0, src, chi, region, eps_scale=False, eps_max=None,
                    conv_threshold=1e-10, max_num_iter=50):
     """Newton iteration of newton_solve (nonlinear_solvers.py:57-115) for one

@@ -14,8 +14,10 @@ The reference's Hz branch calls an unimported ``eye`` (fdfdpy/linalg.py:93);
 the shim sets ``fdfdpy.linalg.eye = scipy.sparse.eye`` (its evident intent).
 
 Outputs (small .npz files beside this script) hold inputs and outputs of
-sfactor/construct_A/derivs/solve_fields/mode sources at sizes that take
-seconds.  Nothing at test time reads the reference.
+sfactor/construct_A/derivs/solve_fields/mode sources and of the Kerr
+solvers (solve_fields_nl, Newton and Born) at sizes that take seconds.
+Nothing at test time reads the reference.  `--only kerr` writes only the
+Kerr fixture.
 """
 from __future__ import annotations
 
@@ -208,8 +210,43 @@ def main():
     M.solver_eigs = orig_eigs
     np.savez_compressed(OUT / "modes.npz", **md)
 
+    kerr_golden()
     print("golden vectors written to", OUT)
 
 
+def kerr_golden():
+    """Kerr solves of the reference (solve_fields_nl -> newton_solve /
+    born_solve, nonlinear_solvers.py:13-115; its complex-to-real Jacobian
+    solves through the pyMKL shim, i.e. exact SuperLU): a 48 x 40 Ez grid
+    with random eps, a 16 x 16 Kerr region and a point source.  Newton at
+    amplitude 3e3 (eps_nl reaches ~10), Born at 3e2 (where the fixed point
+    contracts)."""
+    from fdfdpy import Simulation
+    from fdfdpy.constants import C_0
+    rng = np.random.default_rng(2)
+    Nx, Ny, dl, chi = 48, 40, 0.02, 2.8e-18
+    omega = 2 * np.pi * C_0 / 1.55e-6
+    eps = 1 + 11 * rng.random((Nx, Ny))
+    region = np.zeros((Nx, Ny))
+    region[16:32, 12:28] = 1
+    out = {"eps": eps, "region": region, "omega": omega, "dl": dl, "chi": chi, "npml": np.array([6, 6])}
+    for solver, amp, iters in (("newton", 3e3, 50), ("born", 3e2, 200)):
+        sim = Simulation(omega, eps, dl, [6, 6], "Ez")
+        sim.src[10, 20] = amp
+        sim.add_nl(chi, region)
+        _, _, Ez, conv = sim.solve_fields_nl(solver_nl=solver, conv_threshold=1e-12, max_num_iter=iters)
+        out[f"{solver}_amp"] = amp
+        out[f"{solver}_Ez"] = Ez
+        out[f"{solver}_conv"] = np.asarray(conv).reshape(-1)
+    np.savez_compressed(OUT / "kerr48.npz", **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--only", "kerr"]:
+        install_shims()
+        import warnings
+        warnings.simplefilter("ignore")
+        kerr_golden()
+        print("Kerr golden vectors written to", OUT)
+    else:
+        main()

@@ -168,3 +168,26 @@ def test_mode_operator_and_eigenpair(tag, pol, average):
     assert abs(vals[0] - m[tag + "_eigval"][0]) <= 1e-10 * abs(vals[0])
     v, w = vecs[:, 0], m[tag + "_eigvec"][:, 0]
     assert min(np.linalg.norm(v - w), np.linalg.norm(v + w)) < 1e-8
+
+
+@pytest.mark.parametrize("solver", ["newton", "born"])
+def test_kerr_oracle_matches_reference(solver):
+    """The oracle's Newton and Born iterations (oracle/fdfd_oracle.py) against
+    the reference's solve_fields_nl on a 48 x 40 Ez grid: same iterates
+    (convergence history) and the same final field."""
+    g = np.load(GOLD / "kerr48.npz")
+    eps, region = g["eps"], g["region"]
+    Nx, Ny = eps.shape
+    omega, dl, chi = float(g["omega"]), float(g["dl"]), float(g["chi"])
+    src = np.zeros((Nx, Ny))
+    src[10, 20] = float(g[f"{solver}_amp"])
+    fn = O.newton_kerr_Ez if solver == "newton" else O.born_kerr_Ez
+    E, conv = fn(omega, Nx * dl, Ny * dl, eps, [6, 6], 1e-6, src, chi / 1e-12, region, conv_threshold=1e-12,
+                 max_num_iter=50 if solver == "newton" else 200)
+    ref = g[f"{solver}_Ez"].reshape(-1)
+    assert np.linalg.norm(E - ref) / np.linalg.norm(ref) < 1e-10
+    cref = g[f"{solver}_conv"]
+    cref = cref[cref > 0]
+    assert len(conv) == len(cref)
+    big = cref > 1e-9  # the last steps are at rounding level
+    assert np.allclose(np.asarray(conv)[big], cref[big], rtol=1e-6)
