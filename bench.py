@@ -9,33 +9,52 @@ reference's shapes (there is no dataset).
 One step = one complete solve: operator assembly + multifrontal factor +
 solve + FP64 iterative refinement to a relative residual <= 1e-10, with
 eps and the source already resident in HBM.  The headline is the mixed
-form (complex64 factor + FP64 refinement); the plain complex128 LU is
-measured beside it.  `e2e` repeats the mixed solve through the public API
-(Simulation(...).solve_fields) from host numpy arrays, including the
-host->device upload of eps and the source and the device->host read of the
-three fields.
+form (complex64 factor, tensor-core Schur update, FP64 refinement); the
+plain complex128 LU is measured beside it.  `e2e` repeats the mixed solve
+through the public API (Simulation(...).solve_fields) from host numpy
+arrays, including the host->device upload of eps and the source and the
+device->host read of the three fields.  The line also carries:
+  * the field error of both forms against the reference's own solution of
+    this workload (its default solver path, refined in FP64 with its own
+    factor), from the committed sampled fixture tests/golden/hz2048.npz;
+  * the serving stream (mixed grid sizes, polarizations and right-hand-side
+    counts), closed loop, for the mixed and the plain form: capacity in
+    solves/s, p50/p99 latency, and the mixed-over-plain ratio.
+
+--impl reference times the reference's CPU path (construct_A + SuperLU
+spsolve + field recovery, restated in oracle/ and pinned there to the
+reference's own outputs) on the same workload, without loading this
+package or its library.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W]
-       [--impl ours|reference] [--size S] [--no-plain]
-Multi-GPU: replicas only (every rank runs its own workload; no collective).
+       [--impl ours|reference] [--size S] [--no-plain] [--no-serving]
+Multi-GPU: replicas only (every rank runs its own workload; no collective
+on the data path, one scalar max over ranks for the timing).
 """
 from __future__ import annotations
 
-import argparse
-import json
 import os
-import subprocess
 import sys
-import threading
-import time
 
-import numpy as np
+# SuperLU (the CPU baseline) is single-threaded; a multi-threaded BLAS under
+# it only spins on its small dense calls.  Set before numpy loads.
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+
+import argparse  # noqa: E402
+import json  # noqa: E402
+import subprocess  # noqa: E402
+import threading  # noqa: E402
+import time  # noqa: E402
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "solves/s at rel. residual <=1e-10 (mixed-prec c64+FP64-IR vs plain c128 LU)"
 UNIT = "solves/s"
+GOLDEN_2048 = os.path.join(ROOT, "tests", "golden", "hz2048.npz")
 
 
 def workload(N=2048):
@@ -46,9 +65,16 @@ def workload(N=2048):
     return eps, src
 
 
-def omega():
-    from fdfdpy_gb300.constants import C_0
+def omega_of(C_0):
     return 2 * np.pi * C_0 / 1.55e-6
+
+
+def config(size, world):
+    return {"workload": f"Hz {size}x{size} dl=0.01 NPML=[20,20], eps 16x16 blocks of {{1,12.25}} seed 0, "
+                        f"src[30,:]=1; one step = assemble + factor + solve + FP64 refinement to rel. residual "
+                        f"<= 1e-10",
+            "l2": "256 MB buffer written between timed steps (working set also >> L2)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 class ClockSampler:
@@ -102,7 +128,10 @@ def schur_work(sym, elem=8, nb=64, tc_only=True):
     panel, t = m - k0 - w.  Levels factored whole in shared memory are left
     out (the engine's default rule: at most 64 pivots, the padded front in
     220 KB, and at most 128 rows on levels of 2048 or more fronts); with
-    tc_only, so are the levels below 192 rows (SIMT form)."""
+    tc_only, so are the levels below 192 rows (SIMT form).  Also returns
+    the blocking-independent bytes of the same fronts: each front's
+    update region read and written once (elem * 2 (m - k0)^2 at its first
+    panel)."""
     info = sym.info
     p = sym.export(0, info.n_fronts).astype(np.int64)
     m = sym.export(1, info.n_fronts).astype(np.int64)
@@ -123,7 +152,8 @@ def schur_work(sym, elem=8, nb=64, tc_only=True):
         t = np.where(w > 0, m - k0 - w, 0)
         flops += float(np.sum(8.0 * w * t * t))
         byts += float(np.sum(elem * (2.0 * t * t + 2.0 * t * w)))
-    return flops, byts
+    once = float(np.sum(elem * 2.0 * (m - np.minimum(p, nb)) ** 2))
+    return flops, byts, once
 
 
 # DRAM bytes measured by ncu on one k_schur_tc launch of this workload (the
@@ -134,14 +164,49 @@ def schur_work(sym, elem=8, nb=64, tc_only=True):
 TC_TRAFFIC_RATIO = 545.79 / 590.85
 
 
+def projection_vectors(n, count, seed=2048):
+    """The seeded complex Gaussian vectors of the hz2048 fixture (the same
+    generator as tests/golden/make_golden.py)."""
+    rng = np.random.default_rng(seed)
+    for _ in range(count):
+        g = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        yield g / np.sqrt(2.0)
+
+
+def field_error_vs_reference(fields):
+    """Relative error of (Ex, Ey, Hz) (host arrays, flattened) against the
+    reference's refined solution of the 2048^2 workload: the maximum
+    relative error over the fixture's sampled entries (scaled by the field's
+    RMS) and the projection estimate of ||f - f_ref|| / ||f_ref|| over the
+    seeded Gaussian vectors."""
+    if not os.path.exists(GOLDEN_2048):
+        return None
+    g = np.load(GOLDEN_2048)
+    names = ("Ex", "Ey", "Hz")
+    n = fields[0].size
+    proj = np.zeros((g["proj"].shape[0], 3), dtype=np.complex128)
+    for k, v in enumerate(projection_vectors(n, g["proj"].shape[0])):
+        proj[k] = [v @ f for f in fields]
+    out = {"reference": "reference solve_fields (exact LU) + 3 FP64 refinement steps with its own factor; "
+                        "relres raw %.2e, refined %.2e" % (g["relres"][0], g["relres"][-1])}
+    for j, nm in enumerate(names):
+        rms = g["norms"][j] / np.sqrt(n)
+        samp = float(np.max(np.abs(fields[j][g["sample"]] - g[nm])) / rms)
+        est = float(np.linalg.norm(proj[:, j] - g["proj"][:, j]) / np.linalg.norm(g["proj"][:, j]))
+        out[nm] = {"projection_estimate": est, "sampled_max_over_rms": samp}
+    return out
+
+
 def run_ours(args, rank, world):
     import torch
     from fdfdpy_gb300 import engine, Simulation, _native as NAT
+    from fdfdpy_gb300.constants import C_0
+    from fdfdpy_gb300.replicas import barrier
     torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
     dev = engine.device()
     N = args.size
     eps_h, src_h = workload(N)
-    om = omega()
+    om = omega_of(C_0)
     dl = 0.01
     st = torch.cuda.current_stream()
 
@@ -160,8 +225,7 @@ def run_ours(args, rank, world):
         for _ in range(warmup):
             x = one(fac, prec)
         torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+        barrier()
         ms = 0.0
         for _ in range(steps):
             flush.zero_()
@@ -189,12 +253,20 @@ def run_ours(args, rank, world):
     NAT.call("fdfd_profile_enable", 0)
     res["profile"] = prof
 
+    def host_fields(x):
+        f1, f2 = op.fields(x)
+        return [a.reshape(-1) for a in engine.to_host(f1, f2, x)]
+
+    if N == 2048:
+        res["field_err_vs_reference"] = {"mixed": field_error_vs_reference(host_fields(x64))}
     if not args.no_plain:
         psteps = max(1, min(args.steps, 2))
         fac128, x128, ms128 = timed("c128", psteps, 1)
         res["plain_ms"] = ms128 / psteps
         res["stats128"] = fac128.stats()
         res["field_err_vs_c128"] = float(torch.linalg.vector_norm(x64 - x128) / torch.linalg.vector_norm(x128))
+        if N == 2048:
+            res["field_err_vs_reference"]["plain_c128"] = field_error_vs_reference(host_fields(x128))
         del fac128
     res["launches_per_step"] = launches_mixed / (args.steps + args.warmup)
 
@@ -220,26 +292,95 @@ def run_ours(args, rank, world):
     return res
 
 
-def cpu_baseline_sample(n_side=512):
-    """The reference's CPU path (oracle port: construct_A + SuperLU spsolve)
-    on the same workload family at n_side^2, timed on this host; returned
-    with the solves/s extrapolated to 2048^2 by the ratio of factor flops."""
+def reference_solve(N, with_fields=True):
+    """The reference's CPU path for the workload at N x N (oracle restatement
+    of construct_A, SuperLU spsolve as solver_direct(solver='scipy'), field
+    recovery), timed; returns (seconds, relative residual)."""
     from oracle import fdfd_oracle as O
-    from fdfdpy_gb300 import engine
-    eps, src = workload(n_side)
-    om = omega()
+    eps, src = workload(N)
+    om = omega_of(O.C_0)
+    b = (1j * om * src).reshape(-1)
     t0 = time.perf_counter()
-    A = O.construct_A(om, n_side * 0.01, n_side * 0.01, eps, [20, 20], "Hz", 1e-6)
-    x = O.solve(A, (1j * om * src).reshape(-1))
+    A = O.construct_A(om, N * 0.01, N * 0.01, eps, [20, 20], "Hz", 1e-6)
+    x = O.solve(A, b)
+    if with_fields:
+        O.fields(om, N * 0.01, N * 0.01, eps, [20, 20], "Hz", 1e-6, x)
     dt = time.perf_counter() - t0
-    f_small = engine.Symbolic(n_side, n_side).info.factor_flops
-    f_big = engine.Symbolic(2048, 2048).info.factor_flops
-    return dt, dt * f_big / f_small, x
+    return dt, float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+
+
+def cpu_sample(sizes=(256, 512), target=2048):
+    """A bounded sample of the reference's CPU path: the same workload family
+    at the given sizes; the time at `target` is extrapolated with the power
+    law t ~ N^a fitted to the two sample times (SuperLU's own scaling, no
+    model of this engine)."""
+    ts = [reference_solve(s)[0] for s in sizes]
+    a = float(np.log(ts[1] / ts[0]) / np.log(sizes[1] / sizes[0]))
+    t_target = ts[1] * (target / sizes[1]) ** a
+    return ts, a, t_target
+
+
+def run_reference(args):
+    """The reference arm: its CPU path (oracle restatement pinned to the
+    reference's outputs; SuperLU is single-threaded) on the full workload,
+    one timed solve when it fits the run, else the bounded sample."""
+    N = args.size
+    ts, a, t_pred = cpu_sample((args.cpu_sample // 2, args.cpu_sample), N)
+    cap = float(os.environ.get("FDFD_REF_MAX_S", "1500"))
+    full = 2.0 * t_pred <= cap
+    if full:
+        dt, rel = reference_solve(N)
+        steps, value = 1, 1.0 / dt
+        sample = (f"one complete {N}x{N} solve (construct_A restatement + scipy SuperLU spsolve, the reference's "
+                  f"solver='scipy' path, + field recovery): {dt:.1f} s, rel. residual {rel:.2e}; steps = solves "
+                  f"actually timed (a direct solve has no smaller unit)")
+    else:
+        dt, steps, value = t_pred, 0, 1.0 / t_pred
+        sample = (f"{args.cpu_sample // 2}^2 and {args.cpu_sample}^2 solves of the same workload family "
+                  f"({ts[0]:.1f} s, {ts[1]:.1f} s); {N}^2 time extrapolated with the fitted power law N^{a:.2f} "
+                  f"(a full solve was predicted to exceed {cap:.0f} s)")
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic", "config": config(N, args.gpus),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def serving_stream(n_requests, seed=0):
+    from fdfdpy_gb300.serving import make_stream
+    reqs = make_stream(n_requests=n_requests, rate=1.0, seed=seed, npml=(10, 10), block=8)
+    for r in reqs:
+        r.arrival = 0.0          # closed loop: every request queued at the start
+    return reqs
+
+
+def run_serving_pair(args):
+    """The serving stream (sides {128..1024}, Ez/Hz 50/50, 1-8 complex
+    Gaussian right-hand sides, eps 8x8 blocks, NPML 10, 25% eps reuse),
+    closed loop (all requests queued at t = 0, so solves/s is capacity), for
+    the mixed form and the plain complex128 form on the same requests."""
+    import torch
+    from fdfdpy_gb300.serving import SolveServer
+    from fdfdpy_gb300 import engine
+    warm = serving_stream(6, seed=1)
+    out = {"requests": args.serving_requests,
+           "mode": "closed loop: all requests queued at t=0 (capacity); latency = completion - 0",
+           "workload": "sides {128,256,512,768,1024}, Ez/Hz 50/50, 1-8 complex Gaussian RHS, eps 8x8 blocks "
+                       "of {1,12.25}, NPML 10, 25% eps reuse, seed 0"}
+    for prec in (args.precision, "c128"):
+        SolveServer(slots=args.slots, precision=prec).run(warm, realtime=False)
+        torch.cuda.synchronize()
+        reqs = serving_stream(args.serving_requests)
+        out[prec] = SolveServer(slots=args.slots, precision=prec).run(reqs, realtime=False)
+        engine.release_cached_factors()
+    a, p = out[args.precision], out["c128"]
+    out["speedup_mixed_vs_plain"] = a["solves_per_s"] / p["solves_per_s"] if p["solves_per_s"] else None
+    return out
 
 
 def run_serving(args):
-    """Serving stream: Poisson arrivals, sides {128..1024}, Ez/Hz 50/50,
-    1-8 complex Gaussian RHS, eps 8x8 blocks, NPML 10, 25% eps reuse."""
+    """Serving stream with Poisson arrivals at --rate (offered load)."""
     import torch
     from fdfdpy_gb300.serving import SolveServer, make_stream
     reqs = make_stream(n_requests=args.requests, rate=args.rate, seed=0, npml=(10, 10), block=8)
@@ -247,7 +388,7 @@ def run_serving(args):
     SolveServer(slots=args.slots, precision=args.precision).run(warm, realtime=False)
     torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
-        summ = SolveServer(slots=args.slots, precision=args.precision).run(reqs, realtime=True)
+        summ = SolveServer(slots=args.slots, precision=args.precision).run(reqs, realtime=args.rate > 0)
     return {"metric": "serving solves/s with p50/p99 latency at rel. residual <=1e-10", "value": summ["solves_per_s"],
             "unit": "solves/s", "higher_is_better": True, "dtype": "c64+f64" if args.precision != "c128" else "c128",
             "data": "synthetic", "n_gpus": 1,
@@ -262,13 +403,14 @@ def run_adjoint(args):
     U[1,12], src (100,300), J = |Ez(500,300)|^2; forward + backward timed."""
     import torch
     from fdfdpy_gb300.adjoint import solve_ez
+    from fdfdpy_gb300.constants import C_0
     rng = np.random.default_rng(0)
     N = 600
     eps = np.ones((N, N))
     eps[200:400, 200:400] = rng.uniform(1, 12, size=(200, 200))
     src = np.zeros((N, N))
     src[100, 300] = 1
-    om = omega()
+    om = omega_of(C_0)
     s = torch.tensor(src, device="cuda")
     times = []
     for i in range(args.warmup + args.steps):
@@ -289,19 +431,71 @@ def run_adjoint(args):
             "ms_per_step": 1e3 / v}
 
 
+def run_peaks(args):
+    """Peak arithmetic rates of this GPU for the roofline denominators that
+    the driver does not measure: cuBLAS GEMMs (torch.matmul) of 8192^3 in
+    float32 with TF32 tensor cores, float32 without them (FFMA), and float64
+    (DFMA / FP64 pipe); best of 10 back-to-back launches timed with CUDA
+    events.  Also a device-to-device copy (read + write bytes)."""
+    import torch
+    out = {"metric": "peak rates (cuBLAS GEMM 8192^3, best of 10; copy 2 GiB)", "n_gpus": 1, "data": "synthetic"}
+    n = 8192
+    for name, dtype, tf32 in (("tf32_tflops", torch.float32, True), ("fp32_tflops", torch.float32, False),
+                              ("fp64_tflops", torch.float64, False)):
+        torch.backends.cuda.matmul.allow_tf32 = tf32
+        a = torch.randn(n, n, dtype=dtype, device="cuda")
+        b = torch.randn(n, n, dtype=dtype, device="cuda")
+        c = a @ b
+        best = float("inf")
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            c = torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = 2.0 * n ** 3 / (best * 1e-3) / 1e12
+        del a, b, c
+    torch.backends.cuda.matmul.allow_tf32 = False
+    x = torch.empty(1 << 28, dtype=torch.float64, device="cuda").fill_(1.0)
+    y = torch.empty_like(x)
+    best = float("inf")
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        y.copy_(x)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    out["copy_gbs"] = 2.0 * x.numel() * 8 / (best * 1e-3) / 1e9
+    return out
+
+
+def conv_summary(conv, tol=1e-10):
+    """Newton history (zero-padded; a NaN change counts as an iteration)."""
+    conv = np.asarray(conv, dtype=np.float64).reshape(-1)
+    done = np.flatnonzero(conv != 0)       # NaN != 0 is True
+    iters = int(done[-1] + 1) if done.size else 0
+    last = float(conv[iters - 1]) if iters else 0.0
+    nan = bool(np.isnan(conv[:iters]).any())
+    return {"newton_iters": iters, "final_change": None if np.isnan(last) else last, "nan_iteration": nan,
+            "converged": bool(iters and not nan and last < tol)}
+
+
 def run_kerr(args):
     """Kerr Newton: Ez 1024^2, dl 0.02, NPML 20, centred 400^2 eps 12 with
     chi3 2.8e-18 (zero elsewhere); point source amplitudes logspace(2,5,8)
     solved as concurrent requests (one stream each); Newton to 1e-10."""
     import torch
-    import threading
     from fdfdpy_gb300 import Simulation
-    N = 1024
+    from fdfdpy_gb300.constants import C_0
+    N = args.kerr_size
+    c0, r = (N - N * 400 // 1024) // 2, N * 400 // 1024
     eps = np.ones((N, N))
-    eps[312:712, 312:712] = 12
+    eps[c0:c0 + r, c0:c0 + r] = 12
     region = np.zeros((N, N))
-    region[312:712, 312:712] = 1
-    om = omega()
+    region[c0:c0 + r, c0:c0 + r] = 1
+    om = omega_of(C_0)
     amps = np.logspace(2, 5, 8)
     results = {}
 
@@ -309,15 +503,11 @@ def run_kerr(args):
         with torch.cuda.stream(stream):
             sim = Simulation(om, eps, 0.02, [20, 20], "Ez")
             sim.precision = args.precision
-            sim.src[200, 512] = a
+            sim.src[N * 200 // 1024, N // 2] = a
             sim.add_nl(2.8e-18, region)
             t0 = time.perf_counter()
             out = sim.solve_fields_nl(solver_nl="newton", conv_threshold=1e-10, max_num_iter=args.newton_iters)
-            conv = out[3][:, 0]
-            nz = conv[conv > 0]
-            results[k] = {"amplitude": float(a), "newton_iters": int(nz.size),
-                          "final_change": float(nz[-1]) if nz.size else 0.0,
-                          "converged": bool(nz.size and nz[-1] < 1e-10), "s": time.perf_counter() - t0}
+            results[k] = {"amplitude": float(a), **conv_summary(out[3][:, 0]), "s": time.perf_counter() - t0}
 
     streams = [torch.cuda.Stream() for _ in amps]
     t0 = time.perf_counter()
@@ -331,8 +521,8 @@ def run_kerr(args):
     return {"metric": "Kerr Newton solves/s (8 amplitudes as concurrent requests)", "value": len(amps) / wall,
             "unit": "nonlinear solves/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
             "dtype": "c64+f64" if args.precision != "c128" else "c128",
-            "config": {"workload": "Ez 1024x1024 dl 0.02 NPML 20, 400x400 eps 12 chi3 2.8e-18, src (200,512) "
-                                   "amplitudes logspace(2,5,8)", "precision": args.precision},
+            "config": {"workload": f"Ez {N}x{N} dl 0.02 NPML 20, centred eps 12 square ({r}^2) chi3 2.8e-18, "
+                                   f"point source amplitudes logspace(2,5,8)", "precision": args.precision},
             "wall_s": wall, "per_amplitude": [results[k] for k in sorted(results)]}
 
 
@@ -344,63 +534,48 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=512)
-    ap.add_argument("--workload", default="solve", choices=["solve", "serving", "adjoint", "kerr"])
+    ap.add_argument("--workload", default="solve", choices=["solve", "serving", "adjoint", "kerr", "peaks"])
     ap.add_argument("--precision", default="c64tc", choices=["c64tc", "c64", "c128"])
     ap.add_argument("--method", default="ir", choices=["ir", "gmres"])
     ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--serving-requests", type=int, default=128)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--newton-iters", type=int, default=30)
+    ap.add_argument("--kerr-size", type=int, default=1024)
     args = ap.parse_args()
-    if args.workload != "solve" and args.impl == "ours":
-        fn = {"serving": run_serving, "adjoint": run_adjoint, "kerr": run_kerr}[args.workload]
-        print(json.dumps(fn(args)))
-        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        times = []
-        for i in range(args.warmup + args.steps):
-            dt, ext, _ = cpu_baseline_sample(args.cpu_sample)
-            if i >= args.warmup:
-                times.append(ext)
-        v = 1.0 / float(np.mean(times))
-        sample = (f"{args.cpu_sample}x{args.cpu_sample} Hz solve of the same workload family (oracle port: "
-                  f"construct_A restatement + scipy SuperLU spsolve, the reference's solver='scipy' path), "
-                  f"time extrapolated to 2048x2048 by the nested-dissection factor-flop ratio")
-        print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
-                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-                          "data": "synthetic",
-                          "config": {"workload": f"Hz 2048x2048 dl=0.01 NPML=[20,20] eps 16x16 blocks {{1,12.25}} seed 0, src[30,:]=1"},
-                          "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
-                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if args.workload != "solve":
+        fn = {"serving": run_serving, "adjoint": run_adjoint, "kerr": run_kerr, "peaks": run_peaks}[args.workload]
+        print(json.dumps(fn(args)))
         return
 
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     res = run_ours(args, rank, world)
-    ms = res["mixed_ms"]
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from fdfdpy_gb300.replicas import max_over_ranks
+    import torch
+    ms = max_over_ranks(res["mixed_ms"], device=torch.device("cuda", torch.cuda.current_device()))
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        serving = run_serving_pair(args)
     if rank != 0:
         return
     value = world * 1e3 / ms
     prof = res["profile"]
     tc = args.precision == "c64tc"
     schur_ms, schur_n = prof["schur"] if tc else prof["schur_simt"]
-    fl, by = schur_work(res["sym"], 16 if args.precision == "c128" else 8, tc_only=tc)
+    fl, by, once = schur_work(res["sym"], 16 if args.precision == "c128" else 8, tc_only=tc)
     achieved = by / (schur_ms * 1e-3) / 1e9 if schur_ms > 0 else None
-    peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peaks = json.load(f)
@@ -409,19 +584,17 @@ def main():
         peak, peak_src = 6800.0, "fallback"
     cpu = None
     if os.environ.get("FDFD_BENCH_NO_CPU") != "1":
-        dt, ext, _ = cpu_baseline_sample(args.cpu_sample)
-        cpu = {"value": 1.0 / ext, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{args.cpu_sample}^2 Hz solve, same workload family, {dt:.1f} s; "
-                         f"extrapolated to 2048^2 by the factor-flop ratio (SuperLU is single-threaded)"}
+        ts, a, t_pred = cpu_sample((args.cpu_sample // 2, args.cpu_sample), args.size)
+        cpu = {"value": 1.0 / t_pred, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_sample // 2}^2 and {args.cpu_sample}^2 Hz solves of the same workload family "
+                         f"(construct_A restatement + SuperLU spsolve + field recovery: {ts[0]:.2f} s, {ts[1]:.2f} s); "
+                         f"{args.size}^2 time extrapolated with the fitted power law N^{a:.2f} "
+                         f"(SuperLU is single-threaded)"}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c128" if args.precision == "c128" else "c64+f64", "data": "synthetic",
-        "config": {"workload": f"Hz {args.size}x{args.size} dl=0.01 NPML=[20,20], eps 16x16 blocks of {{1,12.25}} "
-                               f"seed 0, src[30,:]=1; one step = assemble + factor + solve + FP64 refinement "
-                               f"to rel. residual <= 1e-10",
-                   "l2": "256 MB buffer written between timed steps (working set also >> L2)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": config(args.size, world),
         "plain_c128": None if "plain_ms" not in res else {
             "value": 1e3 / res["plain_ms"], "unit": UNIT, "ms_per_step": res["plain_ms"],
             "rel_residual": res["stats128"]["rel_residual"], "refine_iters": res["stats128"]["refine_iters"]},
@@ -429,6 +602,7 @@ def main():
         "mixed": {"rel_residual": res["stats64"]["rel_residual"], "refine_iters": res["stats64"]["refine_iters"],
                   "tiny_pivots": res["stats64"]["tiny_pivots"],
                   "field_err_vs_c128": res.get("field_err_vs_c128")},
+        "field_err_vs_reference": res.get("field_err_vs_reference"),
         "roofline": {"kernel": ("Schur-complement update k_schur_tc (tcgen05 kind::tf32, 3xTF32), the levels "
                                "of fronts with m >= 192" if tc
                                else "Schur-complement update: k_schur_simt (SIMT complex)"),
@@ -439,9 +613,13 @@ def main():
                                                                       and args.precision == "c64tc") else None,
                      "peak_source": f"{peak_src} HBM copy bandwidth",
                      "algorithmic_bytes_per_step": by, "algorithmic_flops_per_step": fl,
+                     "blocking_independent_bytes_per_step": once,
+                     "frac_vs_blocking_independent_bytes": (once / (schur_ms * 1e-3) / 1e9 / peak)
+                     if schur_ms > 0 else None,
                      "useful_tflops": fl / (schur_ms * 1e-3) / 1e12 if schur_ms > 0 else None,
                      "launches_per_step": schur_n, "ms_per_step": schur_ms},
         "kernel_classes_ms": {k: round(v[0], 3) for k, v in prof.items()},
+        "serving": serving,
         "cpu_baseline": cpu,
         "e2e": {"value": 1.0 / res["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"]},

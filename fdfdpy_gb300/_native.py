@@ -18,6 +18,7 @@ FDFD_ERR_CUDA = 3
 FDFD_ERR_SINGULAR_PIVOT = 4
 FDFD_ERR_NOT_CONVERGED = 5
 FDFD_ERR_NO_DEVICE = 6
+FDFD_ERR_TIMEOUT = 7
 
 POL = {"Ez": 0, "Hz": 1}
 PREC = {"c128": 0, "c64": 1, "c64tc": 2}
@@ -31,6 +32,10 @@ class FDFDError(RuntimeError):
 
 class NotConverged(FDFDError):
     pass
+
+
+class DeviceTimeout(FDFDError):
+    """A bounded device-side wait ran out; the call's result is not valid."""
 
 
 class Operator(C.Structure):
@@ -91,6 +96,7 @@ SIGNATURES = {
     "fdfd_factor_stats_get": (C.c_int, [P, C.POINTER(FactorStats)]),
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
     "fdfd_factor_set_fused_limit": (C.c_int, [P, I32]),
+    "fdfd_factor_set_wait_limit": (C.c_int, [P, I64]),
     "fdfd_factor_destroy": (None, [P]),
     "fdfd_profile_enable": (C.c_int, [I32]),
     "fdfd_profile_reset": (C.c_int, []),
@@ -134,6 +140,8 @@ def check(code, what=""):
     msg = lib().fdfd_last_error().decode(errors="replace")
     if code == FDFD_ERR_NOT_CONVERGED:
         raise NotConverged(code, msg)
+    if code == FDFD_ERR_TIMEOUT:
+        raise DeviceTimeout(code, f"{what}: {msg}" if what else msg)
     raise FDFDError(code, f"{what}: {msg}" if what else msg)
 
 

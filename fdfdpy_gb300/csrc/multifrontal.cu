@@ -1589,7 +1589,10 @@ struct fdfd_factor {
     unsigned long long *d_maxdiag = nullptr;
     int *d_tiny = nullptr;
     double *h_norm = nullptr;  // pinned
-    int *h_err = nullptr;      // pinned copy of the solve error flag
+    int *h_err = nullptr;      // pinned copy of the solve error flag (and of the tensor-core one)
+    // polls of the cooperative solves' bounded waits before they give up
+    // (0: the built-in limits; fdfd_factor_set_wait_limit)
+    int64_t wait_limit = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     // cooperative per-level solves (levels with many panel steps)
     std::vector<char> coop_level;
@@ -1810,7 +1813,9 @@ struct GridBar {
 };
 constexpr unsigned kBarLimit = 1u << 24;
 
-__device__ bool grid_sync(GridBar *gb, int *err) {
+// `limit`: polls before giving up (kBarLimit by default; a factor's wait
+// limit, fdfd_factor_set_wait_limit, replaces it).
+__device__ bool grid_sync(GridBar *gb, int *err, unsigned limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1824,7 +1829,7 @@ __device__ bool grid_sync(GridBar *gb, int *err) {
             atomicAdd(&gb->gen, 1u);
         } else {
             for (unsigned int it = 0; *vgen == g; ++it) {
-                if (it > kBarLimit) {
+                if (it >= limit) {
                     ok = 0;
                     atomicExch(err, 1);
                     break;
@@ -1851,6 +1856,14 @@ __device__ bool grid_sync(GridBar *gb, int *err) {
 // a failure, the CTA records the error and the block returns.
 constexpr unsigned kFlagLimit = 1u << 22;
 constexpr unsigned kUnset32 = 0x7fa5a5a5u;
+
+// The limits a factor's cooperative solves use (its wait limit, if set).
+unsigned bar_limit_of(const fdfd_factor *fac) {
+    return fac->wait_limit > 0 ? (unsigned)std::min<int64_t>(fac->wait_limit, kBarLimit) : kBarLimit;
+}
+unsigned flag_limit_of(const fdfd_factor *fac) {
+    return fac->wait_limit > 0 ? (unsigned)std::min<int64_t>(fac->wait_limit, kFlagLimit) : kFlagLimit;
+}
 constexpr unsigned long long kUnset64 = 0x7ff4a5a5a5a5a5a5ull;
 
 __device__ __forceinline__ void set_unset(c64 *p) {
@@ -1896,7 +1909,8 @@ __device__ __forceinline__ bool try_take(const c128 *p, c128 &out) {
 // Stage one published panel (nrhs x w values at vsrc[r * sum_m + c0 + i])
 // into vs (nrhs x NB, zero past w), waiting for each value.
 template <typename T>
-__device__ bool take_panel(const T *vsrc, int64_t sum_m, int c0, int w, int nrhs, T *vs, int *err) {
+__device__ bool take_panel(const T *vsrc, int64_t sum_m, int c0, int w, int nrhs, T *vs, int *err,
+                           unsigned limit) {
     int fail = 0;
     for (int idx = threadIdx.x; idx < nrhs * NB && !fail; idx += blockDim.x) {
         const int r = idx / NB, i = idx % NB;
@@ -1904,7 +1918,7 @@ __device__ bool take_panel(const T *vsrc, int64_t sum_m, int c0, int w, int nrhs
         if (i < w) {
             const T *src = vsrc + r * sum_m + c0 + i;
             for (unsigned it = 0; !try_take(src, v); ++it) {
-                if (it > kFlagLimit || ((it & 1023u) == 1023u && *(volatile int *)err != 0)) {
+                if (it >= limit || ((it & 1023u) == 1023u && *(volatile int *)err != 0)) {
                     fail = 1;
                     atomicExch(err, 1);
                     break;
@@ -1938,7 +1952,7 @@ __device__ __forceinline__ c128 ldcg_c<c128>(const c128 *p) {
 template <typename T>
 __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool live, int k_first, int k_last,
                                             int k_step, int p, const T *vsrc, int64_t sum_m, int nrhs, int *err,
-                                            T *vs, T (&acc)[8]) {
+                                            unsigned flag_limit, T *vs, T (&acc)[8]) {
     const int rr = threadIdx.x >> 2, t0 = 16 * (threadIdx.x & 3);
     // the tile of the next panel is loaded while this panel waits and computes
     T a[16], an[16];
@@ -1958,7 +1972,7 @@ __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool
             for (int i = 0; i < 16; ++i)
                 an[i] = (live && t0 + i < wn) ? F[(r0 + rr) + (int64_t)(cn + t0 + i) * ld] : czero<T>();
         }
-        if (!take_panel(vsrc, sum_m, c0, w, nrhs, vs, err)) return false;
+        if (!take_panel(vsrc, sum_m, c0, w, nrhs, vs, err, flag_limit)) return false;
         for (int r = 0; r < nrhs; ++r) {
             const T *vr = vs + r * NB + t0;
 #pragma unroll
@@ -2008,7 +2022,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
-                int *err, const int2 *__restrict__ units, int nunits) {
+                int *err, const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
     // gather: right-hand side of the pivots and the children's updates; the
@@ -2038,7 +2052,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
             __syncthreads();
         }
     }
-    if (!grid_sync(gb, err)) return;
+    if (!grid_sync(gb, err, bar_limit)) return;
     (void)maxp;
     (void)maxm;
     // pipelined panels: unit (front, row block R); a pivot block computes
@@ -2066,7 +2080,8 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         if (piv) stage_diag<T, false>(F, ld, r0, rn, Ds);
         T acc[8];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-        if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs, err, vin, acc))
+        if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs, err, flag_limit, vin,
+                         acc))
             return;
         quad_reduce(acc, nrhs);
         if (piv) {
@@ -2092,7 +2107,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
                 T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
-                const int2 *__restrict__ units, int nunits) {
+                const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
@@ -2123,7 +2138,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         }
         __syncthreads();
     }
-    if (!grid_sync(gb, err)) return;
+    if (!grid_sync(gb, err, bar_limit)) return;
     // opener, pass 2: acc = y - sum of the column blocks, in a fixed order;
     // the pivot slots of Y are then marked unpublished (x goes there)
     const int prow2 = (maxp + kRowsPerCta - 1) / kRowsPerCta;
@@ -2142,7 +2157,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
             }
         }
     }
-    if (!grid_sync(gb, err)) return;
+    if (!grid_sync(gb, err, bar_limit)) return;
     // pipelined panels, descending: x_R = inv(U_RR) (acc_R - sum_{j>R} U[R, j] x_j),
     // published in Y's pivot rows (and written to the global solution)
     T *Ds = xs, *vin = xs + NB * NB;
@@ -2164,7 +2179,8 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         stage_diag<T, true>(F, ld, r0, rn, Ds);
         T acc[8];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, Y + f.voff, sum_m, nrhs, err, vin, acc))
+        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, Y + f.voff, sum_m, nrhs, err, flag_limit, vin,
+                         acc))
             return;
         quad_reduce(acc, nrhs);
         if (live && q == 0)
@@ -2238,10 +2254,11 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             int *err = fac->d_solve_err;
             const int2 *units = fac->d_units + fac->unit_fwd_off[L];
             int nunits = fac->unit_fwd_n[L];
+            unsigned bar_limit = bar_limit_of(fac), flag_limit = flag_limit_of(fac);
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
                             (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err,
-                            (void *)&units, (void *)&nunits};
+                            (void *)&units, (void *)&nunits, (void *)&bar_limit, (void *)&flag_limit};
             // grid: the most work items any phase of this level has, capped
             // at the co-resident limit
             const int items = std::max(nfl, nunits);
@@ -2288,10 +2305,12 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             T *scr = (T *)fac->d_coop_scratch;
             const int2 *units = fac->d_units + fac->unit_bwd_off[L];
             int nunits = fac->unit_bwd_n[L];
+            unsigned bar_limit = bar_limit_of(fac), flag_limit = flag_limit_of(fac);
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxpp, (void *)&maxb,
                             (void *)&pool, (void *)&fac->d_vars, (void *)&x, (void *)&fac->d_coop_off,
                             (void *)&scr, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
-                            (void *)&gb, (void *)&err, (void *)&units, (void *)&nunits};
+                            (void *)&gb, (void *)&err, (void *)&units, (void *)&nunits, (void *)&bar_limit,
+                            (void *)&flag_limit};
             const int prw = (maxpp + kItemRows - 1) / kItemRows;
             const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
             const int items = std::max(std::max(nfl * prw * cch, nfl), nunits);
@@ -2815,6 +2834,17 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
     CUDA_TRY(cudaEventRecord(fac->ev[1], st));
     fac->coef_op = *op;
     fac->coef_valid = !op->stencil;
+    if (fac->d_tcerr) {
+        // a bounded wait of the tensor-core Schur update that ran out left
+        // tiles without their update: the factor is not valid
+        CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_tcerr, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (*fac->h_err) {
+            fac->numeric_done = false;
+            return fail(FDFD_ERR_TIMEOUT, "factor_numeric: a bounded wait of the tensor-core Schur update ran out "
+                                          "(the factor is not valid)");
+        }
+    }
     fac->numeric_done = true;
     return FDFD_OK;
 }
@@ -2830,6 +2860,21 @@ extern "C" int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x, int32
     int rc = apply_factor(fac, (const double2 *)b, (double2 *)x, nrhs, transpose, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[3], st));
+    // the cooperative substitutions report a bounded wait that ran out in
+    // d_solve_err: read it (one synchronisation of the stream)
+    CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (*fac->h_err)
+        return fail(FDFD_ERR_TIMEOUT, "factor_solve: a bounded wait of the cooperative substitutions ran out (the "
+                                      "solution is not valid)");
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_set_wait_limit(fdfd_factor *fac, int64_t polls) {
+    if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_set_wait_limit: NULL factor");
+    if (polls < 1 && polls != -1)
+        return fail(FDFD_ERR_BAD_ARG, "factor_set_wait_limit: polls must be >= 1 (or -1 for the default)");
+    fac->wait_limit = polls < 0 ? 0 : polls;
     return FDFD_OK;
 }
 
@@ -2876,7 +2921,8 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
         CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (*fac->h_err)
-            return fail(FDFD_ERR_CUDA, "solve_refined: a wait of the cooperative solve timed out");
+            return fail(FDFD_ERR_TIMEOUT, "solve_refined: a bounded wait of the cooperative substitutions ran "
+                                          "out (the solution is not valid)");
         worst = 0.0;
         for (int r = 0; r < nrhs; ++r) {
             const double rel = bnorm[r] > 0 ? fac->h_norm[r] / bnorm[r] : fac->h_norm[r];
@@ -3029,7 +3075,9 @@ extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const
     }
     CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    if (*fac->h_err) return fail(FDFD_ERR_CUDA, "solve_gmres: a wait of the cooperative solve timed out");
+    if (*fac->h_err)
+        return fail(FDFD_ERR_TIMEOUT, "solve_gmres: a bounded wait of the cooperative substitutions ran out (the "
+                                      "solution is not valid)");
     CUDA_TRY(cudaEventRecord(fac->ev[3], st));
     fac->stats.refine_iters = apps - 1;
     fac->stats.rel_residual = rel;

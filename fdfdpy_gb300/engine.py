@@ -293,7 +293,13 @@ class Factor:
         self.handle = h
         N.call("fdfd_factor_set_pivot_tol", h, -1.0 if pivot_tol is None else float(pivot_tol))
         N.call("fdfd_factor_set_fused_limit", h, -1 if fused_max_m is None else int(fused_max_m))
+        N.call("fdfd_factor_set_wait_limit", h, -1)
         self.op = None
+
+    def set_wait_limit(self, polls=None):
+        """Polls a bounded wait of the cooperative substitutions makes before
+        the solve gives up with DeviceTimeout (None: the built-in limits)."""
+        N.call("fdfd_factor_set_wait_limit", self.handle, -1 if polls is None else int(polls))
 
     @staticmethod
     def bytes_needed(sym: Symbolic, precision="c128", max_nrhs=1) -> int:

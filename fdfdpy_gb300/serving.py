@@ -144,8 +144,12 @@ class SolveServer:
             except Exception as e:  # reported per request, the server keeps going
                 req.error = repr(e)
             finally:
-                ent.lock.release()
-            stream.synchronize()
+                # work queued on this stream may still use the factor's solve
+                # workspace: it must finish before another stream takes the factor
+                try:
+                    stream.synchronize()
+                finally:
+                    ent.lock.release()
         with self.cv:
             ent.users -= 1
             if self.cache.get(key) is ent:

@@ -37,6 +37,8 @@ extern "C" {
 #define FDFD_ERR_SINGULAR_PIVOT 4   /* a zero pivot was met (not replaced)  */
 #define FDFD_ERR_NOT_CONVERGED  5   /* refinement hit its iteration cap     */
 #define FDFD_ERR_NO_DEVICE      6   /* no CUDA device visible               */
+#define FDFD_ERR_TIMEOUT        7   /* a bounded device-side wait ran out:
+                                       the result of that call is not valid  */
 
 /* ---- polarizations and precisions ------------------------------------- */
 #define FDFD_POL_EZ 0
@@ -223,10 +225,15 @@ int fdfd_factor_bytes(const fdfd_symbolic *sym, int32_t precision,
                       int32_t max_nrhs, int64_t *bytes);
 int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision,
                        int32_t max_nrhs, fdfd_factor **out);
+/* Returns FDFD_ERR_TIMEOUT (after synchronising the stream) when a bounded
+ * wait of the tensor-core Schur update ran out; the factor then holds no
+ * valid values until the next successful call.                          */
 int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op,
                         void *stream);
 /* One application of the factor: x = A^-1 b (transpose = 0) or
- * x = A^-T b (transpose = 1), complex128 in and out, nrhs columns.       */
+ * x = A^-T b (transpose = 1), complex128 in and out, nrhs columns.
+ * Synchronises the stream to read the substitutions' wait status and
+ * returns FDFD_ERR_TIMEOUT when one of their bounded waits ran out.      */
 int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x,
                       int32_t nrhs, int32_t transpose, void *stream);
 /* Solve with FP64 iterative refinement against the operator `op` until
@@ -237,7 +244,8 @@ int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x,
  * then need a new fdfd_factor_numeric); any other operator is applied
  * matrix-free.  Replaces solver_direct (fdfdpy/linalg.py:122-149).
  * Returns FDFD_ERR_NOT_CONVERGED (x still written) when tol was not
- * reached.                                                               */
+ * reached, FDFD_ERR_TIMEOUT when a bounded wait of the substitutions ran
+ * out (x not valid).                                                     */
 int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op,
                        const void *b, void *x, int32_t nrhs,
                        int32_t transpose, double tol, int32_t max_iter,
@@ -256,6 +264,13 @@ int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol);
  * Takes effect at the next fdfd_factor_numeric.  No counterpart in
  * fdfdpy.                                                                */
 int fdfd_factor_set_fused_limit(fdfd_factor *fac, int32_t max_m);
+/* Polls a bounded wait of the cooperative substitutions (grid barrier,
+ * published panel values) makes before it gives up and the call returns
+ * FDFD_ERR_TIMEOUT; -1 restores the built-in limits (2^24 barrier polls,
+ * 2^22 value polls, each with a short sleep).  For callers that want a
+ * shorter failure detection, and for tests of that path.  Takes effect at
+ * the next solve.  No counterpart in fdfdpy.                             */
+int fdfd_factor_set_wait_limit(fdfd_factor *fac, int64_t polls);
 /* One right-hand side by restarted GMRES(restart) in FP64, right-
  * preconditioned by the factor; stops at ||b - A x|| <= tol ||b|| or after
  * max_iter factor applications (FDFD_ERR_NOT_CONVERGED, x still written).

@@ -1,6 +1,11 @@
 import os
 import sys
 
+# The oracle's SuperLU is single-threaded; a multi-threaded BLAS under it only
+# spins on the small dense calls (two orders of magnitude slower).
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))

@@ -1,9 +1,9 @@
 """Generate golden vectors by running the reference fdfdpy itself.
 
-Run in a container that has the reference checkout (default
-/root/reference, or $FDFDPY_REFERENCE):
+Run where a checkout of the reference is available, naming it with
+``--reference PATH`` (or the environment variable FDFDPY_REFERENCE):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference PATH [--only kerr|hz2048]
 
 The reference imports pyMKL (absent here) and matplotlib (absent); both are
 replaced by sys.modules shims before import:
@@ -17,7 +17,10 @@ Outputs (small .npz files beside this script) hold inputs and outputs of
 sfactor/construct_A/derivs/solve_fields/mode sources and of the Kerr
 solvers (solve_fields_nl, Newton and Born) at sizes that take seconds.
 Nothing at test time reads the reference.  `--only kerr` writes only the
-Kerr fixture.
+Kerr fixture; `--only hz2048` writes the sampled fixture of the 2048 x 2048
+Hz solve (about 15 minutes and 40 GB of host memory: the reference's
+default solver path through the exact-LU shim, then FP64 iterative
+refinement with the same factor).
 """
 from __future__ import annotations
 
@@ -26,15 +29,25 @@ import sys
 import types
 from pathlib import Path
 
+# SuperLU is single-threaded; a multi-threaded BLAS under it only spins on
+# its small dense calls (measured: 107 s against 0.33 s for one 128^2 solve)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+
 import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spl
 
 OUT = Path(__file__).resolve().parent
-REF = os.environ.get("FDFDPY_REFERENCE", "/root/reference")
+REF = os.environ.get("FDFDPY_REFERENCE")
+
+
+LAST_FACTOR = []   # the shim's most recent factor (kept for refinement)
 
 
 def install_shims():
+    if not REF or not Path(REF, "fdfdpy").is_dir():
+        raise SystemExit("name the reference checkout: --reference PATH (or FDFDPY_REFERENCE)")
     pm = types.ModuleType("pyMKL")
 
     class pardisoSolver:  # exact LU stand-in for MKL PARDISO
@@ -43,6 +56,7 @@ def install_shims():
 
         def factor(self):
             self.lu = spl.splu(self.A)
+            LAST_FACTOR[:] = [self.A, self.lu]
 
         def solve(self, b):
             return self.lu.solve(np.asarray(b))
@@ -241,12 +255,85 @@ def kerr_golden():
     np.savez_compressed(OUT / "kerr48.npz", **out)
 
 
+def projection_vectors(n, count, seed=2048):
+    """`count` complex Gaussian vectors of length n with E|g.v|^2 = ||v||^2,
+    generated one after the other from numpy's PCG64 stream (identical on
+    every platform), so a test can rebuild them to estimate a field error
+    from projections."""
+    rng = np.random.default_rng(seed)
+    for _ in range(count):
+        g = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        yield g / np.sqrt(2.0)
+
+
+def hz2048_golden(n_sample=4096, n_proj=8, refine_steps=3):
+    """The large single solve (Hz, 2048 x 2048, dl 0.01, NPML [20, 20],
+    16 x 16 blocks of {1, 12.25} from seed 0, src[30, :] = 1) by the
+    reference's own solve_fields (default solver path: the exact-LU shim),
+    then `refine_steps` FP64 iterative-refinement steps with that same
+    factor; the secondary fields of the refined Hz follow the reference's
+    field recovery (simulation.py:133-160).  Stored: sampled entries of the
+    raw and refined fields, their norms and relative residuals, and the
+    projections of the refined fields on seeded Gaussian vectors."""
+    import time
+    from fdfdpy import Simulation
+    from fdfdpy.constants import C_0, EPSILON_0
+    from fdfdpy.linalg import grid_average
+    N, dl, npml = 2048, 0.01, [20, 20]
+    omega = 2 * np.pi * C_0 / 1.55e-6
+    r0 = np.random.default_rng(0)
+    eps = np.kron(r0.choice([1.0, 12.25], size=(N // 16, N // 16)), np.ones((16, 16)))
+    t0 = time.time()
+    sim = Simulation(omega, eps, dl, npml, "Hz")
+    sim.src[30, :] = 1
+    Ex, Ey, Hz = sim.solve_fields()
+    t_solve = time.time() - t0
+    A, lu = LAST_FACTOR
+    b = (1j * omega * sim.src).reshape(-1).astype(np.complex128)
+    bn = np.linalg.norm(b)
+    x = Hz.reshape(-1).copy()
+    res = [np.linalg.norm(b - A @ x) / bn]
+    for _ in range(refine_steps):
+        x = x + lu.solve(b - A @ x)
+        res.append(np.linalg.norm(b - A @ x) / bn)
+    D = sim.derivs
+    e0 = EPSILON_0 * sim.L0
+    ex_avg = grid_average(e0 * eps, 'x').reshape(-1)
+    ey_avg = grid_average(e0 * eps, 'y').reshape(-1)
+    Exr = 1 / 1j / omega * ((1 / ey_avg) * D['Dyb'].dot(x))
+    Eyr = -1 / 1j / omega * ((1 / ex_avg) * D['Dxb'].dot(x))
+    n = N * N
+    sample = np.sort(np.random.default_rng(7).choice(n, size=n_sample, replace=False))
+    out = {"N": N, "dl": dl, "npml": np.array(npml), "omega": omega, "sample": sample,
+           "raw_Ex": Ex.reshape(-1)[sample], "raw_Ey": Ey.reshape(-1)[sample], "raw_Hz": Hz.reshape(-1)[sample],
+           "raw_norms": np.array([np.linalg.norm(Ex), np.linalg.norm(Ey), np.linalg.norm(Hz)]),
+           "Ex": Exr[sample], "Ey": Eyr[sample], "Hz": x[sample],
+           "norms": np.array([np.linalg.norm(Exr), np.linalg.norm(Eyr), np.linalg.norm(x)]),
+           "relres": np.array(res), "solve_s": t_solve,
+           "raw_vs_refined": np.array([np.linalg.norm(Ex.reshape(-1) - Exr) / np.linalg.norm(Exr),
+                                       np.linalg.norm(Ey.reshape(-1) - Eyr) / np.linalg.norm(Eyr),
+                                       np.linalg.norm(Hz.reshape(-1) - x) / np.linalg.norm(x)])}
+    proj = np.zeros((n_proj, 3), dtype=np.complex128)
+    for k, g in enumerate(projection_vectors(n, n_proj)):
+        proj[k] = [g @ Exr, g @ Eyr, g @ x]
+    out["proj"] = proj
+    np.savez_compressed(OUT / "hz2048.npz", **out)
+    print("hz2048: solve %.1f s, residuals %s" % (t_solve, res))
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--only", "kerr"]:
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="path of the reference checkout")
+    ap.add_argument("--only", default=None, choices=["kerr", "hz2048"])
+    a = ap.parse_args()
+    if a.reference:
+        REF = a.reference
+    if a.only:
         install_shims()
         import warnings
         warnings.simplefilter("ignore")
-        kerr_golden()
-        print("Kerr golden vectors written to", OUT)
+        {"kerr": kerr_golden, "hz2048": hz2048_golden}[a.only]()
+        print("golden vectors written to", OUT)
     else:
         main()

@@ -88,3 +88,34 @@ def test_unconverged_request_is_solved_again_in_complex128():
     assert s["c128_fallbacks"] == len(reqs)
     for r in reqs:
         assert r.fallback and r.rel_residual <= 1e-13, (r.rid, r.rel_residual)
+
+
+def test_tensor_core_requests_alone_equal_mix():
+    """The served headline path (complex64 factor with the tensor-core Schur
+    update, c64tc) on requests large enough to reach the tensor-core levels
+    (fronts of 192 rows or more: 512^2 and 768^2 grids) mixed with small
+    ones: every result meets the residual tolerance and equals the same
+    request solved alone."""
+    from fdfdpy_gb300.serving import SolveServer, make_stream
+    from fdfdpy_gb300 import engine
+
+    def reqs():
+        rs = make_stream(n_requests=6, rate=1e6, sides=(128, 512, 768), reuse=0.2, seed=11, npml=(10, 10))
+        for r in rs:
+            r.arrival = 0.0
+        return rs
+
+    big = [r for r in reqs() if r.eps_r.shape[0] >= 512]
+    assert big and max(engine.symbolic_for(*r.eps_r.shape).info.max_m for r in big) >= 192
+    alone = {}
+    for r in reqs():
+        s = SolveServer(slots=1, precision="c64tc", tol=1e-10).run([r], realtime=False)
+        assert s["failed"] == 0, r.error
+        alone[r.rid] = r.x
+    mix = reqs()
+    s = SolveServer(slots=3, precision="c64tc", tol=1e-10).run(mix, realtime=False)
+    assert s["failed"] == 0, [r.error for r in mix if r.error]
+    assert s["max_rel_residual"] <= 1e-10
+    for r in mix:
+        a = alone[r.rid]
+        assert np.linalg.norm(r.x - a) <= 1e-12 * np.linalg.norm(a), r.rid

@@ -5,8 +5,11 @@ in -- for example a process whose GPU memory is already held by its own
 allocator under a fixed budget.  This test calls it through the C ABI
 twice in a row (the fixed scratch keeps the first call's contents) and
 checks both results against the allocating entry point, fdfd_norms, to the
-tolerance used for the reductions elsewhere (1e-13 relative).  The file
-name makes pytest collect it last.
+tolerance used for the reductions elsewhere (1e-13 relative).  Around each
+allocation-free call it also checks that no device memory was allocated:
+torch's caching allocator and the CUDA runtime's default memory pool (the
+one cudaMallocAsync draws from) hold no more memory after the call than
+before.  The file name makes pytest collect it last.
 """
 import ctypes as C
 
@@ -26,6 +29,18 @@ def _norms(fn, v, n, ncol):
     return np.array(out[:])
 
 
+def _device_memory_in_use():
+    """(torch allocated, torch reserved, default-pool used, default-pool
+    reserved) bytes on the current device."""
+    rt = C.CDLL("libcudart.so.13")             # the runtime the library itself loaded
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), torch.cuda.current_device()) == 0
+    used, reserved = C.c_uint64(), C.c_uint64()
+    assert rt.cudaMemPoolGetAttribute(pool, 0x7, C.byref(used)) == 0       # UsedMemCurrent
+    assert rt.cudaMemPoolGetAttribute(pool, 0x5, C.byref(reserved)) == 0   # ReservedMemCurrent
+    return (torch.cuda.memory_allocated(), torch.cuda.memory_reserved(), used.value, reserved.value)
+
+
 def test_noalloc_norms_match_allocating_entry_point_twice():
     from fdfdpy_gb300 import _native as N
     N.lib()
@@ -34,7 +49,13 @@ def test_noalloc_norms_match_allocating_entry_point_twice():
     for n, ncol in cases:
         h = rng.standard_normal((ncol, n)) + 1j * rng.standard_normal((ncol, n))
         v = torch.from_numpy(h).cuda()
+        torch.cuda.synchronize()
+        before = _device_memory_in_use()
         got = _norms("fdfd_norms_noalloc", v, n, ncol)
+        torch.cuda.synchronize()
+        after = _device_memory_in_use()
+        assert after[0] == before[0] and after[2] == before[2], (before, after)
+        assert after[1] <= before[1] and after[3] <= before[3], (before, after)
         want = _norms("fdfd_norms", v, n, ncol)
         np.testing.assert_allclose(got, want, rtol=1e-13, atol=0)
         np.testing.assert_allclose(got, np.linalg.norm(h, axis=1), rtol=1e-13)
