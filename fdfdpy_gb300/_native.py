@@ -82,6 +82,8 @@ SIGNATURES = {
     "fdfd_adjoint_grad_eps": (C.c_int, [POP, P, P, P, P]),
     "fdfd_mode_stencil": (C.c_int, [I32, I32, I32, P, D, D, D, D, P, P]),
     "fdfd_norms": (C.c_int, [P, I64, I32, P, P]),
+    "fdfd_kerr_assemble": (C.c_int, [I64, P, P, P, D, I32, D, D, D, I32, P, P, P, P, P, P]),
+    "fdfd_flux_probe": (C.c_int, [I32, I32, I32, I32, I32, I32, I32, D, P, P, P, P]),
     "fdfd_norms_noalloc": (C.c_int, [P, I64, I32, P, P]),
     "fdfd_symbolic_create": (C.c_int, [I32, I32, I32, C.POINTER(P)]),
     "fdfd_symbolic_info_get": (C.c_int, [P, C.POINTER(SymbolicInfo)]),

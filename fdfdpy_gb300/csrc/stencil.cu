@@ -276,6 +276,50 @@ __global__ void k_grad_eps(int64_t n, double coef, const double2 *__restrict__ l
     }
 }
 
+// K9 for Hz.  A = Dxf' Tx^-1 Dxb' + Dyf' Ty^-1 Dyb' + omega^2 mu0' I with
+// Tx = diag(eps_x), eps_x = eps0' (eps[i-1, j] + eps[i, j]) / 2 (or eps0' eps
+// without averaging; linalg.py:69-93).  With u = Dxf'^T lambda and
+// v = Dxb' X:  lambda^T (dA / d eps_x[q]) X = -u_q v_q / eps_x[q]^2, so
+//   dL/d eps_r[p] = sum_{q : eps_x[q] depends on eps_r[p]}
+//                   (d eps_x[q] / d eps_r[p]) Re(u_q v_q) / eps_x[q]^2  (+ y)
+// where q ranges over p and its +x (+y) neighbour with averaging (weight
+// eps0'/2 each), over p alone without (weight eps0').
+__device__ __forceinline__ double hz_term_x(const OpDev &o, const double2 *lam, const double2 *X, int i, int j) {
+    const int im = (i == 0) ? o.Nx - 1 : i - 1;
+    const size_t k = (size_t)i * o.Ny + j, km = (size_t)im * o.Ny + j;
+    // u = Dxf'^T lambda at (i, j): column (i, j) of Sxf Dxf
+    const double2 a = c_mul_rn(o.isxf[im], lam[km]), b = c_mul_rn(o.isxf[i], lam[k]);
+    const double2 u = c_scale_rn(c_sub_rn(a, b), o.invdx);
+    const double2 v = c_scale_rn(c_mul_rn(o.isxb[i], c_sub_rn(X[k], X[km])), o.invdx);
+    const double t = inv_eps_x(o, i, j);
+    return (u.x * v.x - u.y * v.y) * t * t;
+}
+__device__ __forceinline__ double hz_term_y(const OpDev &o, const double2 *lam, const double2 *X, int i, int j) {
+    const int jm = (j == 0) ? o.Ny - 1 : j - 1;
+    const size_t k = (size_t)i * o.Ny + j, km = (size_t)i * o.Ny + jm;
+    const double2 a = c_mul_rn(o.isyf[jm], lam[km]), b = c_mul_rn(o.isyf[j], lam[k]);
+    const double2 u = c_scale_rn(c_sub_rn(a, b), o.invdy);
+    const double2 v = c_scale_rn(c_mul_rn(o.isyb[j], c_sub_rn(X[k], X[km])), o.invdy);
+    const double t = inv_eps_y(o, i, j);
+    return (u.x * v.x - u.y * v.y) * t * t;
+}
+
+__global__ void k_grad_eps_hz(OpDev o, const double2 *__restrict__ lam, const double2 *__restrict__ X,
+                              double *__restrict__ g) {
+    const int64_t n = (int64_t)o.Nx * o.Ny;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(k / o.Ny), j = (int)(k % o.Ny);
+        double s = hz_term_x(o, lam, X, i, j) + hz_term_y(o, lam, X, i, j);
+        if (o.averaging) {
+            const int ip = (i == o.Nx - 1) ? 0 : i + 1, jp = (j == o.Ny - 1) ? 0 : j + 1;
+            s += hz_term_x(o, lam, X, ip, j) + hz_term_y(o, lam, X, i, jp);
+            s *= 0.5;
+        }
+        g[k] = o.eps0L * s;
+    }
+}
+
 // ---- norms ----------------------------------------------------------------
 __global__ void k_sumsq_partial(const double2 *__restrict__ v, int64_t n, double *partial) {
     __shared__ double red[kThreads / 32];
@@ -485,8 +529,12 @@ extern "C" int fdfd_adjoint_grad_eps(const fdfd_operator *op, const void *lambda
     if (st) return st;
     if (o.stencil) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: needs the physical operator, not a stencil");
     if (!lambda_ || !E || !grad) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: NULL buffer");
-    if (o.pol != FDFD_POL_EZ) return fail(FDFD_ERR_BAD_ARG, "adjoint_grad_eps: only Ez is supported");
     const int64_t n = (int64_t)o.Nx * o.Ny;
+    if (o.pol == FDFD_POL_HZ) {
+        k_grad_eps_hz<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(o, (const double2 *)lambda_,
+                                                                         (const double2 *)E, grad);
+        return launch_status("adjoint_grad_eps");
+    }
     const double coef = -(o.w2 * o.eps0L);
     k_grad_eps<<<grid_for(n), kThreads, 0, (cudaStream_t)stream>>>(n, coef, (const double2 *)lambda_,
                                                                   (const double2 *)E, grad);

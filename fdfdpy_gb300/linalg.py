@@ -57,22 +57,61 @@ def construct_A(omega, xrange, yrange, eps_r, NPML, pol, L0, averaging=True, tim
     return (A, derivs)
 
 
+def stencil_of_csr(A):
+    """(Nx, Ny, [5][n] coefficients) of a sparse matrix with the periodic
+    5-point pattern of construct_A (every row k = i Ny + j couples to
+    (i -+ 1, j) and (i, j -+ 1) modulo the grid, linalg.py:41-107 and
+    derivatives.py:22-32) -- e.g. A + Anl of simulation.py:125 or any
+    operator a user assembled on that grid -- or None for another pattern.
+    The grid is read off row 0, whose columns are {0, 1, Ny-1, Ny, n-Ny}."""
+    import scipy.sparse as sp
+    if not sp.issparse(A) or A.shape[0] != A.shape[1]:
+        return None
+    A = sp.csr_matrix(A)
+    A.sum_duplicates()
+    A.sort_indices()
+    n = A.shape[0]
+    row0 = A.indices[A.indptr[0]:A.indptr[1]]
+    if n < 9 or len(row0) != 5:
+        return None
+    Ny = int(row0[3])
+    if Ny < 3 or n % Ny or n // Ny < 3 or list(row0) != [0, 1, Ny - 1, Ny, n - Ny]:
+        return None
+    Nx = n // Ny
+    i, j = np.divmod(np.arange(n), Ny)
+    cols = np.stack([i * Ny + j, ((i - 1) % Nx) * Ny + j, ((i + 1) % Nx) * Ny + j,
+                     i * Ny + (j - 1) % Ny, i * Ny + (j + 1) % Ny])
+    vals = np.asarray(A[np.tile(np.arange(n), 5), cols.reshape(-1)]).reshape(5, n).astype(np.complex128)
+    if np.count_nonzero(vals) != A.count_nonzero():
+        return None                                 # entries outside the 5-point pattern
+    return Nx, Ny, vals
+
+
 def solver_direct(A, b, timing=False, solver=DEFAULT_SOLVER, precision=DEFAULT_PRECISION, tol=None,
                   max_iter=None):
     """x = A^-1 b (fdfdpy/linalg.py:122-149) by the GPU multifrontal LU.
 
-    ``A`` must come from ``construct_A`` (it carries its device operator).
-    An all-zero b returns float zeros, as the reference does."""
+    ``A`` from ``construct_A`` carries its device operator and is factored
+    from it; any other sparse matrix with the periodic 5-point pattern of
+    that operator (for instance ``A + Anl``, simulation.py:125) is factored
+    from its five diagonals; other matrices raise ValueError.  An all-zero
+    b returns float zeros, as the reference does."""
     if solver.lower() not in ('pardiso', 'scipy'):
         raise ValueError('Invalid solver choice: {}, options are pardiso or scipy'.format(str(solver)))
     b = np.asarray(b).astype(np.complex128).reshape((-1,))
     if not b.any():
         return np.zeros(b.shape)
+    t = time()
     op = getattr(A, 'fdfd_operator', None)
     if op is None:
-        raise TypeError("solver_direct: A must be built by fdfdpy_gb300 construct_A (its device "
-                        "operator is attached as A.fdfd_operator)")
-    t = time()
+        st = stencil_of_csr(A)
+        if st is None:
+            raise ValueError("solver_direct: the GPU engine factors the periodic 5-point operator of "
+                             "construct_A; this matrix has another sparsity pattern")
+        if A.shape[0] != b.size:
+            raise ValueError("solver_direct: A and b have different sizes")
+        Nx, Ny, vals = st
+        op = engine.StencilOperator(Nx, Ny, engine.as_c128(vals))
     fac = engine.Factor(engine.symbolic_for(op.Nx, op.Ny), precision).numeric(op)
     x = fac.solve(b, tol=DEFAULT_TOL[precision] if tol is None else tol,
                   max_iter=DEFAULT_MAX_REFINE[precision] if max_iter is None else max_iter)

@@ -1,7 +1,6 @@
 """Kerr nonlinear solvers (fdfdpy/nonlinear_solvers.py:13-149) on the GPU.
 
-born_solve  : fixed point E <- (A + Anl(E))^-1 b, refactoring each step
-              (nonlinear_solvers.py:13-54).
+born_solve  : fixed point E <- (A + Anl(E))^-1 b (nonlinear_solvers.py:13-54).
 newton_solve: Newton on f(E) = (A + Anl(E)) E - b with the Jacobian
               J11 = A + Anl + diag(dAde E), J12 = diag(conj(dAde) E),
               dAde = dnl_de omega^2 eps0' (nonlinear_solvers.py:57-149).
@@ -10,54 +9,96 @@ newton_solve: Newton on f(E) = (A + Anl(E)) E - b with the Jacobian
               here the complex factor of J11 preconditions real-inner-product
               GMRES on that real-linear system (solve_complex2real), so the
               Newton loop reuses the same GPU multifrontal engine.
-Both keep E on the device between iterations; the Kerr terms are evaluated
-on the device from the Nonlinearity definitions (nonlinearity.py:18-34).
+
+Factor reuse: neither loop refactors every iteration.  The factor of the
+first iterate's operator (Born: A + Anl; Newton: J11) preconditions
+Jacobian-free GMRES on the current iterate's operator, applied matrix-free
+in FP64; the operator is refactored only when that GMRES needs more than
+`max_inner` factor applications (the iterate has moved far from the
+factored one).  Both keep E on the device between iterations; the Kerr
+terms come from one kernel per nonlinearity (fdfd_kerr_assemble, K1-NL).
 """
 from __future__ import annotations
 
-from copy import deepcopy
+import ctypes as C
 
 import numpy as np
 import torch
 
 from . import engine
-from .constants import EPSILON_0, DEFAULT_TOL, DEFAULT_MAX_REFINE
+from . import _native as N
+from .constants import DEFAULT_TOL, DEFAULT_MAX_REFINE
+
+
+class KerrTerms:
+    """The Kerr nonlinearities of a simulation as device data: for each, chi
+    (already divided by L0^2, simulation.py:72), the region and eps scaling
+    (nonlinearity.py:18-34), evaluated by fdfd_kerr_assemble."""
+
+    def __init__(self, omega, L0, eps_r_dev, nonlinearities):
+        self.omega, self.L0 = float(omega), float(L0)
+        self.eps_r = eps_r_dev.reshape(-1)
+        self.items = []
+        for nli in nonlinearities:
+            if nli.nl_type != 'kerr':
+                raise AssertionError("Only 'kerr' type nonlinearity is supported")
+            region = engine.as_f64(nli.nl_region).reshape(-1)
+            self.items.append((float(nli.chi), region, bool(nli.eps_scale),
+                               float(nli.eps_max) if nli.eps_scale else 0.0))
+
+    @classmethod
+    def of(cls, simulation):
+        return cls(simulation.omega, simulation.L0, simulation._op.eps, simulation.nonlinearity)
+
+    def __call__(self, E, eps_nl=True, jac=False, deps=False, de=False):
+        """Device tensors {'eps_nl', 'jac_diag', 'jac_off', 'dnl_deps',
+        'dnl_de'} (the requested ones) for the device field E (n,)."""
+        E = engine.as_c128(E).reshape(-1)
+        n = E.numel()
+        dev = E.device
+        out = {}
+        if eps_nl:
+            out['eps_nl'] = torch.zeros(n, dtype=torch.float64, device=dev)
+        if deps:
+            out['dnl_deps'] = torch.zeros(n, dtype=torch.float64, device=dev)
+        if de:
+            out['dnl_de'] = torch.zeros(n, dtype=torch.complex128, device=dev)
+        if jac:
+            out['jac_diag'] = torch.zeros(n, dtype=torch.complex128, device=dev)
+            out['jac_off'] = torch.zeros(n, dtype=torch.complex128, device=dev)
+        p = lambda k: engine._ptr(out.get(k))  # noqa: E731
+        for idx, (chi, region, scale, eps_max) in enumerate(self.items):
+            N.call("fdfd_kerr_assemble", n, engine._ptr(E), engine._ptr(self.eps_r), engine._ptr(region), chi,
+                   int(scale), eps_max, self.omega, self.L0, int(idx > 0), p('eps_nl'), p('dnl_deps'),
+                   p('dnl_de'), p('jac_diag'), p('jac_off'), engine.stream_ptr())
+        return out
 
 
 def kerr_terms_device(simulation, E):
     """(eps_nl, dnl_de) on the device for a device field E (n,)."""
-    dev = E.device
-    n = E.numel()
-    eps_nl = torch.zeros(n, dtype=torch.float64, device=dev)
-    dnl_de = torch.zeros(n, dtype=torch.complex128, device=dev)
-    eps_r = engine.as_f64(simulation.eps_r).reshape(-1)
-    for nli in simulation.nonlinearity:
-        if nli.nl_type != 'kerr':
-            raise AssertionError("Only 'kerr' type nonlinearity is supported")
-        region = engine.as_f64(nli.nl_region).reshape(-1)
-        scale = (eps_r - 1) / (nli.eps_max - 1) if nli.eps_scale else 1.0
-        eps_nl = eps_nl + 3 * nli.chi * region * (E.real ** 2 + E.imag ** 2) * scale
-        dnl_de = dnl_de + 3 * nli.chi * region * torch.conj(E) * scale
-    return eps_nl, dnl_de
+    t = KerrTerms.of(simulation)(E, eps_nl=True, de=True)
+    return t['eps_nl'], t['dnl_de']
 
 
-def solve_complex2real(fac, J11_op, J12, f, tol=1e-12, max_iter=400, restart=60):
-    """d with J11 d + J12 * conj(d) = f (J12 a diagonal as an (n,) vector).
+def solve_complex2real(fac, J11_op, J12, f, tol=1e-12, max_iter=400, restart=60, transpose=False):
+    """d with J11 d + J12 * conj(d) = f (J12 a diagonal as an (n,) vector);
+    with transpose, J11^T d + J12 * conj(d) = f.
 
     The operator d -> J11 d + J12 conj(d) is linear over the reals (the
     reference solves it as a real 2n x 2n system, linalg.py:152-186), so
     this is restarted GMRES in the real inner product Re<u, v> on C^n = R^2n,
-    right-preconditioned by the complex factor of J11: d = J11^-1 y.  A plain
-    fixed-point refinement with that factor diverges once |J12| is
-    comparable to J11 (strong Kerr terms); GMRES does not need the
-    contraction.  Every residual is formed in FP64 with the matrix-free
-    J11.  Returns (d, relative residual, operator applications)."""
+    right-preconditioned by the complex factor of J11 (or of a nearby
+    operator): d = J11^-1 y.  A plain fixed-point refinement with that
+    factor diverges once |J12| is comparable to J11 (strong Kerr terms);
+    GMRES does not need the contraction.  Every residual is formed in FP64
+    with the matrix-free J11.  Returns (d, relative residual, operator
+    applications)."""
     fn = float(torch.linalg.vector_norm(f))
     if fn == 0.0:
         return torch.zeros_like(f), 0.0, 0
 
     def op(x):
-        return J11_op.apply(x) + J12 * torch.conj(x)
+        return J11_op.apply(x, transpose=transpose) + J12 * torch.conj(x)
 
     d = torch.zeros_like(f)
     r = f.clone()
@@ -74,7 +115,7 @@ def solve_complex2real(fac, J11_op, J12, f, tol=1e-12, max_iter=400, restart=60)
         g[0] = beta
         k = 0
         for j in range(m):
-            Z[j] = fac.apply_inverse(V[j])
+            Z[j] = fac.apply_inverse(V[j], transpose=transpose)
             w = op(Z[j])
             it += 1
             Vj = V[:j + 1].reshape(j + 1, -1)
@@ -120,18 +161,91 @@ def nl_eq_and_jac(simulation, averaging=True, Ex=None, Ey=None, Ez=None, compute
     device-resident: returns (f (n,), J11 operator, J12 (n,)) or f."""
     if simulation.pol != 'Ez':
         raise ValueError('Invalid polarization: {}'.format(str(simulation.pol)))
-    omega = simulation.omega
-    E = engine.as_c128(Ez).reshape(-1)
-    eps_nl, dnl_de = kerr_terms_device(simulation, E)
-    op_nl = simulation._op.with_terms(eps_add=eps_nl)
-    b = engine.as_c128(simulation.src * 1j * omega).reshape(-1)
+    b = engine.as_c128(simulation.src * 1j * simulation.omega).reshape(-1)
+    return _f_and_jac(simulation._op, b, KerrTerms.of(simulation), engine.as_c128(Ez).reshape(-1), compute_jac)
+
+
+def _f_and_jac(op_lin, b, kerr, E, compute_jac=True):
+    t = kerr(E, eps_nl=True, jac=compute_jac)
+    op_nl = op_lin.with_terms(eps_add=t['eps_nl'])
     fE = -op_nl.residual(E, b)                       # (A + Anl) E - b
     if not compute_jac:
         return fE
-    dAde = dnl_de * (omega ** 2 * EPSILON_0 * simulation.L0)
-    J11 = simulation._op.with_terms(eps_add=eps_nl, diag_add=dAde * E)
-    J12 = torch.conj(dAde) * E
-    return fE, J11, J12
+    J11 = op_lin.with_terms(eps_add=t['eps_nl'], diag_add=t['jac_diag'])
+    return fE, J11, t['jac_off']
+
+
+def _rel_change(E, Eprev):
+    return float(torch.linalg.vector_norm(E - Eprev) / torch.linalg.vector_norm(E))
+
+
+def newton_device(op_lin, b, kerr, E0, precision, conv_threshold=1e-10, max_num_iter=50, lin_tol=1e-11,
+                  reuse_factor=True, max_inner=60, stats=None):
+    """Newton iterations from the device field E0; returns (E, conv_array,
+    factor) with the factor last used (of J11 at some iterate)."""
+    sym = engine.symbolic_for(op_lin.Nx, op_lin.Ny)
+    conv_array = np.zeros((max_num_iter, 1))
+    E = E0
+    fac = None
+    stats = {} if stats is None else stats
+    stats.update(factorizations=0, inner=[], linear_rel_residual=[])
+    convergence = float('inf')
+    for istep in range(max_num_iter):
+        Eprev = E
+        fx, J11, J12 = _f_and_jac(op_lin, b, kerr, Eprev)
+        rel, its, d = 1.0, 0, None
+        if fac is not None and reuse_factor:
+            d, rel, its = solve_complex2real(fac, J11, J12, fx, tol=lin_tol, max_iter=max_inner)
+        if d is None or rel > max(lin_tol, 1e-9):
+            fac = engine.Factor(sym, precision).numeric(J11)
+            stats['factorizations'] += 1
+            d, rel, its2 = solve_complex2real(fac, J11, J12, fx, tol=lin_tol)
+            its += its2
+        stats['inner'].append(its)
+        stats['linear_rel_residual'].append(rel)
+        E = Eprev - d
+        convergence = _rel_change(E, Eprev)
+        conv_array[istep] = convergence
+        if not convergence >= conv_threshold:   # NaN ends the loop too
+            break
+    if not convergence <= conv_threshold:
+        print("the simulation did not converge, reached {}".format(convergence))
+    return E, conv_array, fac
+
+
+def born_device(op_lin, b, kerr, E0, precision, conv_threshold=1e-10, max_num_iter=50, reuse_factor=True,
+                max_inner=30, stats=None):
+    """Born iterations from the device field E0; returns (E, conv_array,
+    factor)."""
+    sym = engine.symbolic_for(op_lin.Nx, op_lin.Ny)
+    conv_array = np.zeros((max_num_iter, 1))
+    E = E0
+    fac = None
+    stats = {} if stats is None else stats
+    stats.update(factorizations=0, inner=[])
+    tol = DEFAULT_TOL[precision]
+    convergence = float('inf')
+    for istep in range(max_num_iter):
+        Eprev = E
+        op = op_lin.with_terms(eps_add=kerr(Eprev)['eps_nl'])
+        E = None
+        if fac is not None and reuse_factor:
+            try:
+                E = fac.solve(b, op=op, method='gmres', tol=tol, max_iter=max_inner, raise_on_fail=True)
+            except N.NotConverged:
+                E = None
+        if E is None:
+            fac = engine.Factor(sym, precision).numeric(op)
+            stats['factorizations'] += 1
+            E = fac.solve(b, op=op, tol=tol, max_iter=DEFAULT_MAX_REFINE[precision])
+        stats['inner'].append(fac.stats()['refine_iters'])
+        convergence = _rel_change(E, Eprev)
+        conv_array[istep] = convergence
+        if not convergence >= conv_threshold:
+            break
+    if not convergence <= conv_threshold:
+        print("the simulation did not converge, reached {}".format(convergence))
+    return E, conv_array, fac
 
 
 def _start_field(simulation, Estart):
@@ -139,60 +253,49 @@ def _start_field(simulation, Estart):
         return engine.as_c128(Estart).reshape(-1)
     if simulation.fields['Ez'] is None:
         simulation.solve_fields()
-    return engine.as_c128(deepcopy(simulation.fields['Ez'])).reshape(-1)
+    return engine.as_c128(simulation.fields['Ez']).reshape(-1)
 
 
-def born_solve(simulation, Estart=None, conv_threshold=1e-10, max_num_iter=50, averaging=True):
-    conv_array = np.zeros((max_num_iter, 1))
+def _rhs(simulation):
+    return engine.as_c128(simulation.src * 1j * simulation.omega).reshape(-1)
+
+
+def born_solve(simulation, Estart=None, conv_threshold=1e-10, max_num_iter=50, averaging=True,
+               reuse_factor=True):
     if simulation.pol != 'Ez':
         raise ValueError('Invalid polarization: {}'.format(str(simulation.pol)))
     Ez = _start_field(simulation, Estart)
-    prec = simulation.precision
-    b = engine.as_c128(simulation.src * 1j * simulation.omega).reshape(-1)
-    convergence = float('inf')
-    for istep in range(max_num_iter):
-        Eprev = Ez
-        eps_nl, _ = kerr_terms_device(simulation, Eprev)
-        op = simulation._op.with_terms(eps_add=eps_nl)
-        fac = engine.Factor(engine.symbolic_for(simulation.Nx, simulation.Ny), prec).numeric(op)
-        Ez = fac.solve(b, tol=DEFAULT_TOL[prec], max_iter=DEFAULT_MAX_REFINE[prec])
-        convergence = float(torch.linalg.vector_norm(Ez - Eprev) / torch.linalg.vector_norm(Ez))
-        conv_array[istep] = convergence
-        if convergence < conv_threshold:
-            break
-    if convergence > conv_threshold:
-        print("the simulation did not converge, reached {}".format(convergence))
-    return _finish(simulation, Ez, conv_array, averaging)
+    kerr = KerrTerms.of(simulation)
+    simulation.nl_stats = {}
+    Ez, conv_array, fac = born_device(simulation._op, _rhs(simulation), kerr, Ez, simulation.precision,
+                                      conv_threshold, max_num_iter, reuse_factor, stats=simulation.nl_stats)
+    return _finish(simulation, Ez, conv_array, averaging, kerr, fac)
 
 
 def newton_solve(simulation, Estart=None, conv_threshold=1e-10, max_num_iter=50, averaging=True,
-                 solver='pardiso', jac_solver='c2r', matrix_format='csr', lin_tol=1e-11):
-    conv_array = np.zeros((max_num_iter, 1))
+                 solver='pardiso', jac_solver='c2r', matrix_format='csr', lin_tol=1e-11, reuse_factor=True):
     if simulation.pol != 'Ez':
         raise ValueError('Invalid polarization: {}'.format(str(simulation.pol)))
     Ez = _start_field(simulation, Estart)
-    prec = simulation.precision
-    sym = engine.symbolic_for(simulation.Nx, simulation.Ny)
-    convergence = float('inf')
-    simulation.newton_stats = []
-    for istep in range(max_num_iter):
-        Eprev = Ez
-        fx, J11, J12 = nl_eq_and_jac(simulation, Ez=Eprev)
-        fac = engine.Factor(sym, prec).numeric(J11)
-        Ediff, rel, its = solve_complex2real(fac, J11, J12, fx, tol=lin_tol)
-        simulation.newton_stats.append({"linear_rel_residual": rel, "inner_iters": its})
-        Ez = Eprev - Ediff
-        convergence = float(torch.linalg.vector_norm(Ez - Eprev) / torch.linalg.vector_norm(Ez))
-        conv_array[istep] = convergence
-        if convergence < conv_threshold:
-            break
-    if convergence > conv_threshold:
-        print("the simulation did not converge, reached {}".format(convergence))
-    return _finish(simulation, Ez, conv_array, averaging)
+    kerr = KerrTerms.of(simulation)
+    simulation.nl_stats = {}
+    Ez, conv_array, fac = newton_device(simulation._op, _rhs(simulation), kerr, Ez, simulation.precision,
+                                        conv_threshold, max_num_iter, lin_tol, reuse_factor,
+                                        stats=simulation.nl_stats)
+    simulation.newton_stats = [{"linear_rel_residual": r, "inner_iters": i}
+                               for r, i in zip(simulation.nl_stats['linear_rel_residual'],
+                                               simulation.nl_stats['inner'])]
+    return _finish(simulation, Ez, conv_array, averaging, kerr, fac)
 
 
-def _finish(simulation, Ez, conv_array, averaging):
-    """Final solve with the converged eps_nl (nonlinear_solvers.py:106-107)."""
-    simulation.compute_nl(Ez.cpu().numpy().reshape(simulation.Nx, simulation.Ny))
-    (Hx, Hy, Ez_out) = simulation.solve_fields(include_nl=True, averaging=averaging)
+def _finish(simulation, Ez, conv_array, averaging, kerr, fac=None):
+    """The final linear solve with the converged eps_nl
+    (nonlinear_solvers.py:106-107, simulation.py:124-126) and the fields;
+    the Kerr terms are evaluated on the device (the simulation's eps_nl,
+    dnl_de and dnl_deps attributes receive host copies)."""
+    t = kerr(Ez, eps_nl=True, deps=True, de=True)
+    simulation._set_nl_device(t['eps_nl'])
+    simulation.dnl_de, simulation.dnl_deps = (a.reshape(simulation.Nx, simulation.Ny)
+                                              for a in engine.to_host(t['dnl_de'], t['dnl_deps']))
+    (Hx, Hy, Ez_out) = simulation.solve_fields(include_nl=True, averaging=averaging, preconditioner=fac)
     return (Hx, Hy, Ez_out, conv_array)

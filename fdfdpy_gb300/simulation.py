@@ -63,14 +63,21 @@ class Simulation:
 
     # ---- nonlinearity (simulation.py:57-73) -------------------------------------
     def compute_nl(self, e, matrix_format=DEFAULT_MATRIX_FORMAT):
-        self.eps_nl = np.zeros(self.eps_r.shape)
-        self.dnl_de = np.zeros(self.eps_r.shape)
-        self.dnl_deps = np.zeros(self.eps_r.shape)
-        for nli in self.nonlinearity:
-            self.eps_nl = self.eps_nl + nli.eps_nl(e, self.eps_r)
-            self.dnl_de = self.dnl_de + nli.dnl_de(e, self.eps_r)
-            self.dnl_deps = self.dnl_deps + nli.dnl_deps(e, self.eps_r)
+        """eps_nl, dnl_de, dnl_deps of the field e (simulation.py:57-68),
+        evaluated on the device by the Kerr kernel (fdfd_kerr_assemble);
+        the attributes hold host copies, as in the reference."""
+        from .nonlinear_solvers import KerrTerms
+        t = KerrTerms.of(self)(e, eps_nl=True, deps=True, de=True)
+        self._set_nl_device(t['eps_nl'])
+        self.dnl_de, self.dnl_deps = (a.reshape(self.Nx, self.Ny) for a in engine.to_host(t['dnl_de'],
+                                                                                          t['dnl_deps']))
+
+    def _set_nl_device(self, eps_nl_dev):
+        """Make a device eps_nl current (host copy in self.eps_nl)."""
         self._nl_version = getattr(self, '_nl_version', 0) + 1
+        self._eps_nl_dev = (self._nl_version, eps_nl_dev.reshape(-1))
+        self.eps_nl = engine.to_host(eps_nl_dev)[0].reshape(self.Nx, self.Ny)
+        self._eps_nl_host_sig = (id(self.eps_nl), hash(self.eps_nl.tobytes()))
 
     @property
     def Anl(self):
@@ -95,6 +102,7 @@ class Simulation:
         self._A_host = None
         self._derivs_host = None
         self._factors = {}
+        self._fields_dev = {}
         self.fields = {f: None for f in _FIELD_NAMES}
         self.fields_nl = {f: None for f in _FIELD_NAMES}
 
@@ -133,17 +141,41 @@ class Simulation:
             self._factors[(key, precision)] = fac
         return fac
 
+    def _eps_nl_device(self):
+        """eps_nl on the device: the kernel's copy while self.eps_nl is the
+        array it produced, else an upload of whatever the user assigned."""
+        dev = getattr(self, '_eps_nl_dev', None)
+        arr = np.ascontiguousarray(self.eps_nl, dtype=np.float64)
+        sig = (id(self.eps_nl), hash(arr.tobytes()))
+        if dev is not None and sig == getattr(self, '_eps_nl_host_sig', None):
+            return dev[1], ('nl', dev[0])
+        return engine.as_f64(arr).reshape(-1), ('nl_host',) + sig
+
     def _operator(self, include_nl):
         if not include_nl:
             return self._op, ('lin',)
-        return (self._op.with_terms(eps_add=np.asarray(self.eps_nl, dtype=np.float64)),
-                ('nl', getattr(self, '_nl_version', 0)))
+        eps_nl, key = self._eps_nl_device()
+        return self._op.with_terms(eps_add=eps_nl), key
 
-    def solve_device(self, b, include_nl=False, precision=None, tol=None, max_iter=None, transpose=False):
+    def solve_device(self, b, include_nl=False, precision=None, tol=None, max_iter=None, transpose=False,
+                     preconditioner=None):
         """Solve A x = b on the device (b: (n,) or (nrhs, n)); returns a
-        complex128 device tensor.  Reuses the cached factor."""
+        complex128 device tensor.  Reuses the cached factor.  With
+        `preconditioner` (a factor of a nearby operator, e.g. the last one of
+        a Kerr loop) the operator is solved by GMRES preconditioned by it and
+        factored only if that does not reach the tolerance."""
         precision = precision or self.precision
         op, key = self._operator(include_nl)
+        tol_ = DEFAULT_TOL[precision] if tol is None else tol
+        if preconditioner is not None and (key, precision) not in self._factors:
+            from . import _native
+            try:
+                x = preconditioner.solve(b, transpose=transpose, op=op, method='gmres', tol=tol_, max_iter=30,
+                                         raise_on_fail=True)
+                self.last_solve_stats = preconditioner.stats()
+                return x
+            except _native.NotConverged:
+                pass
         fac = self._factor_for(op, key, precision)
         method = 'ir' if precision == 'c128' else self.refinement
         x = fac.solve(b, transpose=transpose, op=op, method=method,
@@ -153,7 +185,7 @@ class Simulation:
         return x
 
     def solve_fields(self, include_nl=False, timing=False, averaging=True, solver=DEFAULT_SOLVER,
-                     matrix_format=DEFAULT_MATRIX_FORMAT, precision=None, tol=None):
+                     matrix_format=DEFAULT_MATRIX_FORMAT, precision=None, tol=None, preconditioner=None):
         if solver.lower() not in ('pardiso', 'scipy'):
             raise ValueError('Invalid solver choice: {}, options are pardiso or scipy'.format(str(solver)))
         if self.pol not in ('Ez', 'Hz'):
@@ -169,10 +201,11 @@ class Simulation:
             X = torch.zeros(Nx * Ny, dtype=torch.complex128, device=engine.device())
             zero_src = True
         else:
-            X = self.solve_device(b, include_nl=include_nl, precision=precision, tol=tol)
+            X = self.solve_device(b, include_nl=include_nl, precision=precision, tol=tol,
+                                  preconditioner=preconditioner)
             zero_src = False
         if include_nl:
-            eps_dev = engine.as_f64(self.eps_r + self.eps_nl).reshape(-1)
+            eps_dev = self._op.eps + self._eps_nl_device()[0]
         else:
             eps_dev = self._op.eps if self.pol == 'Hz' else None
         f1, f2 = self._op.fields(X, averaging=averaging, eps=eps_dev)
@@ -184,6 +217,9 @@ class Simulation:
             F1, F2, F3 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2, X))
         if timing:
             print('Linear system solve took {:.2f} seconds'.format(time() - t))
+        # device copies of the fields, tied to the host arrays returned now
+        names = ('Ex', 'Ey', 'Hz') if self.pol == 'Hz' else ('Hx', 'Hy', 'Ez')
+        self._fields_dev[bool(include_nl)] = {nm: (d, id(h)) for nm, d, h in zip(names, (f1, f2, X), (F1, F2, F3))}
         if self.pol == 'Hz':
             if not include_nl:
                 self.fields['Ex'], self.fields['Ey'], self.fields['Hz'] = F1, F2, F3
@@ -215,34 +251,46 @@ class Simulation:
         assert self.NPML[0] >= 0 and self.NPML[1] >= 0, "both elements of NPML must be >= 0"
         assert self.pol in ['Ez', 'Hz'], "pol must be one of 'Ez' or 'Hz'"
 
-    # ---- flux (simulation.py:260-315), host reduction on a line -----------------
+    # ---- flux (simulation.py:260-315): a device reduction ------------------------
     def flux_probe(self, direction_normal, center, width, nl=False):
+        """Poynting flux through a line of cells normal to `direction_normal`
+        (simulation.py:260-315), reduced on the device (fdfd_flux_probe)
+        from the fields of the last solve (or the arrays in self.fields /
+        self.fields_nl if they were set by hand).  Returns a float."""
+        out = self.flux_probe_device(direction_normal, center, width, nl=nl)
+        return float(out.item())
+
+    def flux_probe_device(self, direction_normal, center, width, nl=False):
+        """As flux_probe, the result left on the device (a 0-d float64
+        tensor), for loops that should not synchronise."""
+        from . import _native
         if direction_normal == "x":
-            inds_x = [center[0], center[0] + 1]
-            inds_y = [int(center[1] - width / 2), int(center[1] + width / 2)]
+            normal, i0, j0 = 0, int(center[0]), int(center[1] - width / 2)
+            length = int(center[1] + width / 2) - j0
         elif direction_normal == "y":
-            inds_x = [int(center[0] - width / 2), int(center[0] + width / 2)]
-            inds_y = [center[1], center[1] + 1]
+            normal, i0, j0 = 1, int(center[0] - width / 2), int(center[1])
+            length = int(center[0] + width / 2) - i0
         else:
             raise ValueError("The value of direction_normal is neither x nor y!")
         flds = self.fields_nl if nl else self.fields
-        sx = slice(inds_x[0], inds_x[1] + 1)
-        sy = slice(inds_y[0], inds_y[1] + 1)
-        cx = slice(inds_x[0], inds_x[1])
-        cy = slice(inds_y[0], inds_y[1])
-        if self.pol == 'Ez':
-            Ez, Hx, Hy = flds['Ez'], flds['Hx'], flds['Hy']
-            if direction_normal == "x":
-                Ez_x = grid_average(Ez[sx, sy], 'x')[:-1, :-1]
-                return self.dl * np.sum(-1 / 2 * np.real(Ez_x * np.conj(Hy[cx, cy])))
-            Ez_y = grid_average(Ez[sx, sy], 'y')[:-1, :-1]
-            return self.dl * np.sum(1 / 2 * np.real(Ez_y * np.conj(Hx[cx, cy])))
-        Hz, Ex, Ey = flds['Hz'], flds['Ex'], flds['Ey']
-        if direction_normal == "x":
-            Hz_x = grid_average(Hz[sx, sy], 'x')[:-1, :-1]
-            return self.dl * np.sum(1 / 2 * np.real(Ey[cx, cy] * np.conj(Hz_x)))
-        Hz_y = grid_average(Hz[sx, sy], 'y')[:-1, :-1]
-        return self.dl * np.sum(-1 / 2 * np.real(Ex[cx, cy] * np.conj(Hz_y)))
+        F, G = ('Ez', 'Hy' if normal == 0 else 'Hx') if self.pol == 'Ez' else ('Hz', 'Ey' if normal == 0 else 'Ex')
+        dev = self._fields_dev.get(bool(nl), {})
+
+        def pick(name):
+            h = flds.get(name)
+            d = dev.get(name)
+            if d is not None and h is not None and d[1] == id(h):
+                return d[0]
+            if h is None:
+                raise ValueError("flux_probe: field {} has not been solved".format(name))
+            return engine.as_c128(h).reshape(-1)
+        Fd, Gd = pick(F), pick(G)
+        out = torch.empty((), dtype=torch.float64, device=Fd.device)
+        if length <= 0:
+            return out.zero_()
+        _native.call("fdfd_flux_probe", self.Nx, self.Ny, _native.POL[self.pol], normal, i0, j0, length,
+                     float(self.dl), engine._ptr(Fd), engine._ptr(Gd), engine._ptr(out), engine.stream_ptr())
+        return out
 
     # ---- design regions (simulation.py:344-369) ---------------------------------
     def init_design_region(self, design_region, eps_m, style=''):
@@ -269,11 +317,35 @@ class Simulation:
         new = cls.__new__(cls)
         memo[id(self)] = new
         for k, v in self.__dict__.items():
-            if k in ('_op', '_factors', '_A_host', '_derivs_host'):
+            if k in ('_op', '_factors', '_A_host', '_derivs_host', '_fields_dev', '_eps_nl_dev'):
                 continue
             setattr(new, k, deepcopy(v, memo))
         new._op = self._op
         new._factors = dict(self._factors)
         new._A_host = None
         new._derivs_host = None
+        new._fields_dev = {}
         return new
+
+    # ---- differentiable solve (no counterpart in the reference) -------------------
+    def solve_fields_torch(self, eps_r=None, precision=None):
+        """The three fields as torch tensors, differentiable in eps_r (a
+        float64 tensor; default: the current eps_r) through the adjoint
+        solve on the forward factor: (Ex, Ey, Hz) for Hz, (Hx, Hy, Ez) for
+        Ez, from the current source.  With nonlinearities added (add_nl,
+        Ez), the Kerr field by Newton and its adjoint."""
+        from . import adjoint
+        prec = precision or self.precision
+        e = torch.as_tensor(np.asarray(self.eps_r) if eps_r is None else eps_r, dtype=torch.float64,
+                            device=engine.device())
+        src = torch.as_tensor(np.asarray(self.src), device=e.device)
+        if self.nonlinearity:
+            if self.pol != 'Ez':
+                raise ValueError('Invalid polarization: {}'.format(str(self.pol)))
+            from .nonlinear_solvers import KerrTerms  # noqa: F401  (checks the nonlinearity types)
+            X = adjoint._KerrSolve.apply(e, src, self.omega, self.dl, self.NPML, self.L0, self.nonlinearity,
+                                         prec, 1e-12, 50)
+        else:
+            X = adjoint.solve(e, src, self.omega, self.dl, self.NPML, self.pol, self.L0, prec)
+        f1, f2 = adjoint.secondary_fields(X, e, self.omega, self.dl, self.NPML, self.pol, self.L0)
+        return (f1, f2, X)

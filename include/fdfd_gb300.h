@@ -143,11 +143,54 @@ int fdfd_mode_stencil(int32_t N, int32_t pol, int32_t average,
                       double L0, double shift, void *out, void *stream);
 
 /* ---- K9: adjoint gradient ----------------------------------------------
- * dL/d(eps_r) = -omega^2 * eps0 * L0 * Re(lambda * E) (Ez), written to
- * grad (n float64).  No counterpart in the reference (it has no
- * derivative w.r.t. eps); derived from fdfdpy/linalg.py:53-54,66.       */
+ * dL/d(eps_r) for a real loss L of the solved primary field E, given the
+ * adjoint field lambda = A^-T conj(dL/dE) (torch's complex gradient
+ * convention), written to grad (n float64):
+ *   Ez: -omega^2 * eps0 * L0 * Re(lambda * E)  (A's eps term is diagonal,
+ *       fdfdpy/linalg.py:53-54,66);
+ *   Hz: sum over the edge permittivities eps_x, eps_y that depend on the
+ *       cell (grid-averaged, linalg.py:73-78, or not) of
+ *       d eps_edge/d eps_r * Re((Df'^T lambda)(Db' E)) / eps_edge^2
+ *       (A's eps terms Dxf' Tx^-1 Dxb' + Dyf' Ty^-1 Dyb', linalg.py:86-93).
+ * No counterpart in the reference (it has no derivative w.r.t. eps).    */
 int fdfd_adjoint_grad_eps(const fdfd_operator *op, const void *lambda_,
                           const void *E, double *grad, void *stream);
+
+/* ---- K1-NL: Kerr terms ---------------------------------------------------
+ * One pass over n cells for one Kerr nonlinearity (chi already divided by
+ * L0^2, as Simulation.add_nl stores it), replacing the numpy evaluation of
+ * fdfdpy/nonlinearity.py:18-34, their sum in Simulation.compute_nl
+ * (fdfdpy/simulation.py:57-68) and the Jacobian terms of nl_eq_and_jac
+ * (fdfdpy/nonlinear_solvers.py:117-149).  With s = (eps_r - 1)/(eps_max - 1)
+ * when eps_scale != 0, else 1:
+ *   eps_nl   = 3 chi region |E|^2 s                          (float64)
+ *   dnl_deps = 3 chi region |E|^2 / (eps_max - 1), or 0      (float64)
+ *   dnl_de   = 3 chi region conj(E) s                        (complex128)
+ *   jac_diag = dAde * E,  jac_off = conj(dAde) * E           (complex128)
+ *   with dAde = dnl_de * omega^2 eps0 L0.
+ * Every output pointer may be NULL (not written); accumulate != 0 adds to
+ * the outputs (several nonlinearities) instead of overwriting them.
+ * E: complex128 (device); eps_r (needed with eps_scale), region: float64. */
+int fdfd_kerr_assemble(int64_t n, const void *E, const double *eps_r,
+                       const double *region, double chi, int32_t eps_scale,
+                       double eps_max, double omega, double L0,
+                       int32_t accumulate, double *eps_nl, double *dnl_deps,
+                       void *dnl_de, void *jac_diag, void *jac_off,
+                       void *stream);
+
+/* ---- flux probe ----------------------------------------------------------
+ * Replaces Simulation.flux_probe (fdfdpy/simulation.py:260-315) as a device
+ * reduction over one line of cells.  normal = 0 (x): the line is
+ * (i0, j0 .. j0+len-1) and F is averaged with (i0+1, j); normal = 1 (y): the
+ * line is (i0 .. i0+len-1, j0), averaged with (i, j0+1).  F is the field
+ * the reference averages (Ez for pol Ez, Hz for pol Hz), G its partner
+ * (Hy / Hx for Ez, Ey / Ex for Hz, x / y normal).  Writes to *out (device
+ * double): dl * c * sum Re(avg(F) conj(G)), c = -1/2 (Ez, x), +1/2 (Ez, y),
+ * +1/2 (Hz, x), -1/2 (Hz, y).  The line and the averaging neighbour must
+ * lie inside the grid (FDFD_ERR_BAD_ARG otherwise).                      */
+int fdfd_flux_probe(int32_t Nx, int32_t Ny, int32_t pol, int32_t normal,
+                    int32_t i0, int32_t j0, int32_t len, double dl,
+                    const void *F, const void *G, double *out, void *stream);
 
 /* ---- reductions --------------------------------------------------------
  * Column 2-norms of a complex128 (n x ncol) array, written to host array

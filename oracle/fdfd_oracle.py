@@ -300,6 +300,57 @@ def adjoint_grad_eps_Ez(A, E, g, omega, L0):
     return -(omega ** 2) * (EPSILON_0 * L0) * np.real(lam * E.reshape(-1))
 
 
+def adjoint_grad_eps_Hz(omega, xlen, ylen, eps_r, NPML, L0, E, g, averaging=True):
+    """Reference gradient dL/d(eps_r) for Hz (derived from construct_A,
+    linalg.py:69-93: A = Dxf' Tx^-1 Dxb' + Dyf' Ty^-1 Dyb' + omega^2 mu0' I
+    with Tx, Ty the grid-averaged eps0' eps), by the chain rule through the
+    edge permittivities with scipy's sparse derivative operators:
+    lambda = A^-T conj(g), u = Dxf'^T lambda, v = Dxb' E,
+    dL/d eps_x[q] = Re(u_q v_q) / eps_x[q]^2, spread onto eps_r by the
+    averaging weights (1/2 on the cell and its -x neighbour)."""
+    eps_r = np.asarray(eps_r, dtype=np.float64)
+    Nx, Ny = eps_r.shape
+    A = construct_A(omega, xlen, ylen, eps_r, NPML, 'Hz', L0, averaging=averaging)
+    lam = spl.spsolve(A.T.tocsc(), np.conj(np.asarray(g)).reshape(-1))
+    D = derivs(omega, xlen, ylen, Nx, Ny, NPML, L0)
+    E = np.asarray(E).reshape(-1)
+    e = EPSILON_0 * L0 * eps_r
+    ex = grid_average(e, 'x') if averaging else e
+    ey = grid_average(e, 'y') if averaging else e
+    tx = (np.real((D['Dxf'].T @ lam) * (D['Dxb'] @ E)) / ex.reshape(-1) ** 2).reshape(Nx, Ny)
+    ty = (np.real((D['Dyf'].T @ lam) * (D['Dyb'] @ E)) / ey.reshape(-1) ** 2).reshape(Nx, Ny)
+    if averaging:
+        grad = 0.5 * EPSILON_0 * L0 * (tx + np.roll(tx, -1, axis=0) + ty + np.roll(ty, -1, axis=1))
+    else:
+        grad = EPSILON_0 * L0 * (tx + ty)
+    return grad.reshape(-1)
+
+
+def kerr_adjoint_grad_Ez(omega, xlen, ylen, eps_r, NPML, L0, E, g, chi, region, eps_scale=False, eps_max=None):
+    """Reference gradient dL/d(eps_r) at a converged Kerr solution E of
+    (A + diag(w eps_nl(E))) E = b (w = omega^2 eps0 L0; newton_solve,
+    nonlinear_solvers.py:57-115): the real 2n x 2n Newton Jacobian R of
+    solver_complex2real (linalg.py:152-186) is transposed, R^T m = [Re g;
+    Im g] is solved by SuperLU, mu = m_r + i m_i, and
+    dL/d eps_p = -w Re(conj(mu_p) (1 + dnl_deps_p) E_p)."""
+    eps_r = np.asarray(eps_r, dtype=np.float64)
+    E = np.asarray(E).reshape(-1)
+    n = E.size
+    w = omega ** 2 * EPSILON_0 * L0
+    A = construct_A(omega, xlen, ylen, eps_r, NPML, 'Ez', L0)
+    eps_nl, dnl = kerr_terms(E, eps_r.reshape(-1), chi, np.asarray(region).reshape(-1), eps_scale, eps_max)
+    dAde = dnl * w
+    J11 = (A + sp.diags(w * eps_nl) + sp.diags(dAde * E)).tocsr()
+    J12 = sp.diags(np.conj(dAde) * E).tocsr()
+    R = sp.vstack((sp.hstack((J11.real + J12.real, -J11.imag + J12.imag)),
+                   sp.hstack((J11.imag + J12.imag, J11.real - J12.real)))).tocsc()
+    g = np.asarray(g).reshape(-1)
+    m = spl.spsolve(R.T.tocsc(), np.concatenate([g.real, g.imag]))
+    mu = m[:n] + 1j * m[n:]
+    deps = 3 * chi * np.asarray(region).reshape(-1) * np.abs(E) ** 2 / (eps_max - 1) if eps_scale else 0.0
+    return -w * np.real(np.conj(mu) * (1 + deps) * E)
+
+
 # ---- mode source (fdfdpy/source/mode.py:62-108) ------------------------------
 def mode_operator(pol, eps_slice, omega, dl, L0, average):
     """The 1-D periodic slice operator of insert_mode (mode.py:76-91):

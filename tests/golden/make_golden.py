@@ -20,7 +20,8 @@ Nothing at test time reads the reference.  `--only kerr` writes only the
 Kerr fixture; `--only hz2048` writes the sampled fixture of the 2048 x 2048
 Hz solve (about 15 minutes and 40 GB of host memory: the reference's
 default solver path through the exact-LU shim, then FP64 iterative
-refinement with the same factor).
+refinement with the same factor); `--only kerr_sweep` the Kerr Newton
+amplitude sweep at 128 x 128 (a few minutes).
 """
 from __future__ import annotations
 
@@ -255,6 +256,37 @@ def kerr_golden():
     np.savez_compressed(OUT / "kerr48.npz", **out)
 
 
+def kerr_sweep_golden(N=128, n_sample=2048):
+    """The Kerr Newton workload (Ez, dl 0.02, NPML [20, 20], a centred
+    square of eps 12 and chi3 2.8e-18 covering 400/1024 of the side, point
+    source at (200/1024, 1/2) of the grid, amplitudes logspace(2, 5, 8)) at
+    N x N, solved by the reference's own solve_fields_nl (Newton, its
+    complex-to-real Jacobian solves through the exact-LU shim), 50
+    iterations at most, threshold 1e-10.  Stored per amplitude: the
+    convergence history and sampled entries (and the norm) of the final Ez."""
+    from fdfdpy import Simulation
+    from fdfdpy.constants import C_0
+    omega = 2 * np.pi * C_0 / 1.55e-6
+    r = N * 400 // 1024
+    c0 = (N - r) // 2
+    eps = np.ones((N, N))
+    eps[c0:c0 + r, c0:c0 + r] = 12
+    region = np.zeros((N, N))
+    region[c0:c0 + r, c0:c0 + r] = 1
+    amps = np.logspace(2, 5, 8)
+    sample = np.sort(np.random.default_rng(3).choice(N * N, size=n_sample, replace=False))
+    out = {"N": N, "amps": amps, "sample": sample, "src_ij": np.array([N * 200 // 1024, N // 2])}
+    for k, a in enumerate(amps):
+        sim = Simulation(omega, eps, 0.02, [20, 20], "Ez")
+        sim.src[N * 200 // 1024, N // 2] = a
+        sim.add_nl(2.8e-18, region)
+        _, _, Ez, conv = sim.solve_fields_nl(solver_nl="newton", conv_threshold=1e-10, max_num_iter=50)
+        out[f"conv_{k}"] = np.asarray(conv).reshape(-1)
+        out[f"Ez_{k}"] = Ez.reshape(-1)[sample]
+        out[f"norm_{k}"] = np.linalg.norm(Ez)
+    np.savez_compressed(OUT / f"kerr{N}_sweep.npz", **out)
+
+
 def projection_vectors(n, count, seed=2048):
     """`count` complex Gaussian vectors of length n with E|g.v|^2 = ||v||^2,
     generated one after the other from numpy's PCG64 stream (identical on
@@ -325,7 +357,7 @@ if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None, help="path of the reference checkout")
-    ap.add_argument("--only", default=None, choices=["kerr", "hz2048"])
+    ap.add_argument("--only", default=None, choices=["kerr", "hz2048", "kerr_sweep"])
     a = ap.parse_args()
     if a.reference:
         REF = a.reference
@@ -333,7 +365,7 @@ if __name__ == "__main__":
         install_shims()
         import warnings
         warnings.simplefilter("ignore")
-        {"kerr": kerr_golden, "hz2048": hz2048_golden}[a.only]()
+        {"kerr": kerr_golden, "hz2048": hz2048_golden, "kerr_sweep": kerr_sweep_golden}[a.only]()
         print("golden vectors written to", OUT)
     else:
         main()

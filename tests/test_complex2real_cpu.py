@@ -14,8 +14,8 @@ class _Op:
     def __init__(self, M):
         self.M = M
 
-    def apply(self, x):
-        return self.M @ x
+    def apply(self, x, transpose=False):
+        return (self.M.T if transpose else self.M) @ x
 
 
 class _ApproxInverse:
@@ -27,8 +27,8 @@ class _ApproxInverse:
         E = eps * (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * np.abs(M).max()
         self.Minv = torch.from_numpy(np.linalg.inv(M + E))
 
-    def apply_inverse(self, v):
-        return self.Minv @ v
+    def apply_inverse(self, v, transpose=False):
+        return (self.Minv.T if transpose else self.Minv) @ v
 
 
 def _real2n(J11, J12, f):
@@ -67,6 +67,21 @@ def test_complex2real_gmres_matches_real_solve():
 def test_complex2real_zero_rhs():
     n = 8
     M = torch.eye(n, dtype=torch.complex128)
-    d, rel, it = solve_complex2real(type("F", (), {"apply_inverse": lambda self, v: v})(), _Op(M),
+    d, rel, it = solve_complex2real(type("F", (), {"apply_inverse": lambda self, v, transpose=False: v})(), _Op(M),
                                     torch.zeros(n, dtype=torch.complex128), torch.zeros(n, dtype=torch.complex128))
     assert it == 0 and rel == 0.0 and not d.any()
+
+
+def test_complex2real_transposed_system():
+    """transpose=True solves J11^T d + J12 conj(d) = f (the Kerr adjoint)
+    with the transposed preconditioner."""
+    rng = np.random.default_rng(8)
+    n = 90
+    J11 = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 12 * np.eye(n)
+    J12 = 3.0 * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+    f = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = _real2n(J11.T, J12, f)
+    M = torch.from_numpy(J11)
+    d, rel, it = solve_complex2real(_ApproxInverse(M, rng, 1e-4), _Op(M), torch.from_numpy(J12), torch.from_numpy(f),
+                                    tol=1e-12, max_iter=400, restart=40, transpose=True)
+    assert rel <= 1e-12 and np.linalg.norm(d.numpy() - ref) <= 1e-9 * np.linalg.norm(ref)

@@ -261,3 +261,21 @@ def test_released_factor_memory_is_reused(eng):
     assert rel(f3.apply_inverse(b).cpu().numpy(), O.solve(A2, b)) < 1e-10
     other = eng.Factor(eng.Symbolic(Nx, Ny), "c128")  # a private analysis never takes a parked factor
     assert other.handle.value != h1
+
+
+@pytest.mark.parametrize("pol", ["Ez", "Hz"])
+def test_solver_direct_general_csr(eng, pol):
+    """solver_direct on a scipy matrix that did not come from construct_A
+    (the reference accepts any sparse A, linalg.py:122-149): A + a random
+    diagonal (the A + Anl of simulation.py:125), assembled on the host by
+    the oracle, is factored from its five diagonals; other patterns raise."""
+    import scipy.sparse as sp
+    from fdfdpy_gb300.linalg import solver_direct
+    eps, A, rng = _problem(40, 33, pol, seed=3)
+    A2 = (A + sp.diags(1e11 * rng.random(A.shape[0]))).tocsr()
+    b = rng.standard_normal(A.shape[0]) + 1j * rng.standard_normal(A.shape[0])
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-8)):
+        x = solver_direct(A2, b, precision=prec)
+        assert rel(x, O.solve(A2, b)) < tol, prec
+    with pytest.raises(ValueError):
+        solver_direct(sp.random(A.shape[0], A.shape[0], 0.01, format="csr") + sp.eye(A.shape[0]), b)
