@@ -329,7 +329,7 @@ def run_reference(args):
     power-law extrapolation, labelled as such."""
     N = args.size
     ts, a, t_pred = cpu_sample((args.cpu_sample // 2, args.cpu_sample), N)
-    cap = float(os.environ.get("FDFD_REF_MAX_S", "1500"))
+    cap = float(os.environ.get("FDFD_REF_MAX_S", "1650"))
     full = None
     try:
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--reference-full-solve", str(N)],
@@ -373,27 +373,40 @@ def run_serving_pair(args):
     the mixed form and the plain complex128 form on the same requests."""
     import torch
     from fdfdpy_gb300.serving import SolveServer, make_stream
+    from fdfdpy_gb300.autotune import Autotuner
     from fdfdpy_gb300 import engine
     warm = serving_stream(6, seed=1)
+    tuner = Autotuner()
     out = {"requests": args.serving_requests,
            "mode": "closed loop: all requests queued at t=0 (capacity; latency = completion - 0); then Poisson "
                    "arrivals at 70% of that capacity (at_70pct_load: latency = completion - arrival)",
            "workload": "sides {128,256,512,768,1024}, Ez/Hz 50/50, 1-8 complex Gaussian RHS, eps 8x8 blocks "
                        "of {1,12.25}, NPML 10, 25% eps reuse, seed 0"}
+    def server(prec):
+        return SolveServer(slots=args.slots, precision=prec, batch_max=args.batch_max,
+                           autotune=tuner if args.batch_max > 1 else None)
     for prec in (args.precision, "c128"):
-        SolveServer(slots=args.slots, precision=prec).run(warm, realtime=False)
+        server(prec).run(warm, realtime=False)
         torch.cuda.synchronize()
         reqs = serving_stream(args.serving_requests)
-        out[prec] = SolveServer(slots=args.slots, precision=prec).run(reqs, realtime=False)
+        t_tune = time.perf_counter()
+        if args.batch_max > 1:
+            for shape in sorted({tuple(r.eps_r.shape) for r in reqs}):
+                tuner.config_for(shape, prec)
+        t_tune = time.perf_counter() - t_tune
+        out[prec] = server(prec).run(reqs, realtime=False)
+        out[prec]["tuning_s"] = t_tune
         engine.release_cached_factors()
         # latency at an offered load of 70% of that capacity (Poisson arrivals)
         rate = 0.7 * out[prec]["requests_per_s"]
         reqs = make_stream(n_requests=args.serving_requests, rate=rate, seed=0, npml=(10, 10), block=8)
-        summ = SolveServer(slots=args.slots, precision=prec).run(reqs, realtime=True)
+        summ = server(prec).run(reqs, realtime=True)
         out[prec]["at_70pct_load"] = {"rate_requests_per_s": rate, "p50_latency_s": summ["p50_latency_s"],
                                       "p99_latency_s": summ["p99_latency_s"], "solves_per_s": summ["solves_per_s"],
                                       "failed": summ["failed"], "max_rel_residual": summ["max_rel_residual"]}
         engine.release_cached_factors()
+    out["autotuned"] = {f"{k[0]}x{k[1]} {k[2]}": {"batch": v["batch"], "fused_max_m": v["fused_max_m"]}
+                        for k, v in tuner.table.items()}
     a, p = out[args.precision], out["c128"]
     out["speedup_mixed_vs_plain"] = a["solves_per_s"] / p["solves_per_s"] if p["solves_per_s"] else None
     return out
@@ -405,17 +418,28 @@ def run_serving(args):
     from fdfdpy_gb300.serving import SolveServer, make_stream
     reqs = make_stream(n_requests=args.requests, rate=args.rate, seed=0, npml=(10, 10), block=8)
     warm = make_stream(n_requests=4, rate=1e6, seed=1, sides=(128, 256), npml=(10, 10), block=8)
-    SolveServer(slots=args.slots, precision=args.precision).run(warm, realtime=False)
+    from fdfdpy_gb300.autotune import Autotuner
+    tuner = Autotuner() if args.batch_max > 1 else None
+
+    def server():
+        return SolveServer(slots=args.slots, precision=args.precision, batch_max=args.batch_max, autotune=tuner)
+    server().run(warm, realtime=False)
+    if tuner is not None:
+        for shape in sorted({tuple(r.eps_r.shape) for r in reqs}):
+            tuner.config_for(shape, args.precision)
     torch.cuda.synchronize()
     with ClockSampler(torch.cuda.current_device()) as clk:
-        summ = SolveServer(slots=args.slots, precision=args.precision).run(reqs, realtime=args.rate > 0)
+        summ = server().run(reqs, realtime=args.rate > 0)
     return {"metric": "serving solves/s with p50/p99 latency at rel. residual <=1e-10", "value": summ["solves_per_s"],
             "unit": "solves/s", "higher_is_better": True, "dtype": "c64+f64" if args.precision != "c128" else "c128",
             "data": "synthetic", "n_gpus": 1,
             "config": {"workload": f"{args.requests} requests, Poisson rate {args.rate}/s, sides 128..1024, "
                                    f"Ez/Hz 50/50, 1-8 RHS, eps 8x8 blocks, NPML 10, 25% eps reuse",
-                       "slots": args.slots, "precision": args.precision},
-            "serving": summ, "clocks": clk.summary()}
+                       "slots": args.slots, "precision": args.precision, "batch_max": args.batch_max},
+            "serving": summ, "clocks": clk.summary(),
+            "autotuned": None if tuner is None else {f"{k[0]}x{k[1]} {k[2]}": {"batch": v["batch"],
+                                                                               "fused_max_m": v["fused_max_m"]}
+                                                     for k, v in tuner.table.items()}}
 
 
 def run_adjoint(args):
@@ -563,6 +587,7 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=128)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--batch-max", type=int, default=8, help="problems per forest factorization (1: none)")
     ap.add_argument("--newton-iters", type=int, default=30)
     ap.add_argument("--kerr-size", type=int, default=1024)
     ap.add_argument("--reference-full-solve", type=int, default=0, help=argparse.SUPPRESS)

@@ -86,6 +86,7 @@ SIGNATURES = {
     "fdfd_flux_probe": (C.c_int, [I32, I32, I32, I32, I32, I32, I32, D, P, P, P, P]),
     "fdfd_norms_noalloc": (C.c_int, [P, I64, I32, P, P]),
     "fdfd_symbolic_create": (C.c_int, [I32, I32, I32, C.POINTER(P)]),
+    "fdfd_symbolic_create_batch": (C.c_int, [I32, I32, I32, I32, C.POINTER(P)]),
     "fdfd_symbolic_info_get": (C.c_int, [P, C.POINTER(SymbolicInfo)]),
     "fdfd_symbolic_export": (C.c_int, [P, I32, P]),
     "fdfd_symbolic_destroy": (None, [P]),
@@ -95,6 +96,8 @@ SIGNATURES = {
     "fdfd_factor_solve": (C.c_int, [P, P, P, I32, I32, P]),
     "fdfd_solve_refined": (C.c_int, [P, POP, P, P, I32, I32, D, I32, P]),
     "fdfd_solve_gmres": (C.c_int, [P, POP, P, P, I32, D, I32, I32, P]),
+    "fdfd_factor_numeric_batch": (C.c_int, [P, POP, I32, P]),
+    "fdfd_solve_refined_batch": (C.c_int, [P, P, P, I32, D, I32, P, P]),
     "fdfd_factor_stats_get": (C.c_int, [P, C.POINTER(FactorStats)]),
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
     "fdfd_factor_set_fused_limit": (C.c_int, [P, I32]),

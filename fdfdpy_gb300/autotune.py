@@ -1,0 +1,126 @@
+"""The engine's own autotuner (no counterpart in the reference).
+
+For a grid shape and precision it picks, by timing on the device, the
+launch configuration of the serving path:
+
+* the batch size B: how many operators of that grid one forest
+  factorization takes (BatchFactor: every level's front updates of all B
+  problems in one launch), and
+* the whole-front limit (the largest front the one-launch dense LU kernel
+  takes; larger fronts go through the per-panel TRSM / Schur tiles).
+
+Each candidate factors B synthetic operators of the grid (eps_r in 8 x 8
+blocks of {1, 12.25}, the serving workload's family) and refines `nrhs`
+right-hand sides per problem; the score is right-hand sides solved per
+second of device time (CUDA events).  Results are cached per (shape,
+precision) in memory and, when `path` is given, in a JSON file that later
+processes read instead of timing again.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+
+import numpy as np
+import torch
+
+from . import engine
+from .constants import C_0
+
+
+class Autotuner:
+
+    def __init__(self, batches=(1, 2, 4, 8), fused_limits=(-1, 128), nrhs=4, path=None, memory_fraction=0.25,
+                 pol="Hz", npml=(10, 10), dl=0.02):
+        self.batches, self.fused_limits = tuple(batches), tuple(fused_limits)
+        self.nrhs, self.path, self.memory_fraction = int(nrhs), path, float(memory_fraction)
+        self.pol, self.npml, self.dl = pol, tuple(npml), float(dl)
+        self.table: dict = {}
+        self._lock = threading.Lock()
+        if path and os.path.exists(path):
+            with open(path) as f:
+                self.table = {tuple(json.loads(k)): v for k, v in json.load(f).items()}
+
+    # ---- queries -------------------------------------------------------------
+    def config_for(self, shape, precision):
+        key = (int(shape[0]), int(shape[1]), precision)
+        with self._lock:
+            cfg = self.table.get(key)
+        if cfg is None:
+            cfg = self.tune(shape, precision)
+        return cfg
+
+    def batch_for(self, shape, precision):
+        return int(self.config_for(shape, precision)["batch"])
+
+    def fused_for(self, shape, precision):
+        return int(self.config_for(shape, precision)["fused_max_m"])
+
+    # ---- timing --------------------------------------------------------------
+    def _operators(self, shape, B, seed=0):
+        rng = np.random.default_rng(seed)
+        om = 2 * np.pi * C_0 / 1.55e-6
+        Nx, Ny = shape
+        ops = []
+        for _ in range(B):
+            eps = np.kron(rng.choice([1.0, 12.25], size=(-(-Nx // 8), -(-Ny // 8))), np.ones((8, 8)))[:Nx, :Ny]
+            ops.append(engine.DeviceOperator(om, eps, Nx * self.dl, Ny * self.dl, self.npml, self.pol, 1e-6))
+        rhs = [torch.randn(self.nrhs, Nx * Ny, dtype=torch.complex128, device=engine.device()) for _ in range(B)]
+        return ops, rhs
+
+    def _time(self, shape, precision, B, fused, reps=2):
+        sym = engine.symbolic_for(shape[0], shape[1], batch=B)
+        ops, rhs = self._operators(shape, B)
+        if B > 1:
+            fac = engine.BatchFactor(sym, precision, max_nrhs=8, fused_max_m=fused)
+
+            def step():
+                fac.numeric(ops)
+                fac.solve_batch(rhs, tol=1e-10, max_iter=40)
+        else:
+            fac = engine.Factor(sym, precision, max_nrhs=8, fused_max_m=fused)
+
+            def step():
+                fac.numeric(ops[0])
+                fac.solve(rhs[0], tol=1e-10, max_iter=40)
+        step()                                    # warm-up (first touch, module load)
+        st = torch.cuda.current_stream()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            step()
+            e1.record(st)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del fac
+        return best
+
+    def tune(self, shape, precision):
+        """Time every candidate that fits in memory; record and return the
+        fastest {'batch', 'fused_max_m', 'solves_per_s', 'candidates'}."""
+        free, _ = torch.cuda.mem_get_info()
+        results = []
+        for B in self.batches:
+            need = engine.Factor.bytes_needed(engine.symbolic_for(shape[0], shape[1], batch=B), precision, 8)
+            if need > self.memory_fraction * free:
+                continue
+            for fused in self.fused_limits:
+                ms = self._time(shape, precision, B, fused)
+                results.append({"batch": B, "fused_max_m": fused, "ms": ms,
+                                "solves_per_s": 1e3 * B * self.nrhs / ms})
+        engine.release_cached_factors()
+        if not results:
+            results = [{"batch": 1, "fused_max_m": -1, "ms": float("nan"), "solves_per_s": float("nan")}]
+        best = max(results, key=lambda r: r["solves_per_s"] if r["solves_per_s"] == r["solves_per_s"] else -1)
+        cfg = {"batch": best["batch"], "fused_max_m": best["fused_max_m"], "solves_per_s": best["solves_per_s"],
+               "candidates": results}
+        with self._lock:
+            self.table[(int(shape[0]), int(shape[1]), precision)] = cfg
+            if self.path:
+                tmp = self.path + ".tmp"
+                with open(tmp, "w") as f:
+                    json.dump({json.dumps(list(k)): v for k, v in self.table.items()}, f, indent=1)
+                os.replace(tmp, self.path)
+        return cfg

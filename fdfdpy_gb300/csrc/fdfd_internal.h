@@ -21,6 +21,11 @@ int fail(int code, const std::string &msg);
 // Host-side symbolic analysis (symbolic.cpp).  Arrays are host vectors;
 // the factor uploads what it needs.
 struct Symbolic {
+    // A batch symbolic describes `batch` independent copies of one grid's
+    // front tree (a forest): Nx = batch * rows rows of Ny cells, problem b
+    // owning rows [b rows, (b + 1) rows) with its own periodic wrap; level L
+    // holds the batch's copies of the single tree's level-L fronts.
+    int32_t batch = 1, rows = 0;
     int32_t Nx = 0, Ny = 0, leaf_area = 0;
     int32_t nf = 0, nlev = 0;
     std::vector<int32_t> p, m, ld, parent, child0, child1, height, vars_off;
@@ -37,6 +42,8 @@ struct Symbolic {
 };
 
 int build_symbolic(int32_t Nx, int32_t Ny, int32_t leaf_area, Symbolic &S);
+// `batch` copies of S1 as one forest (see Symbolic::batch).
+int replicate_symbolic(const Symbolic &S1, int32_t batch, Symbolic &S);
 
 }  // namespace fdfd
 

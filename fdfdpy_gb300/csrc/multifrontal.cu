@@ -80,14 +80,16 @@ struct FrontD {
 // formulas in FP64, whose rate on this GPU is a small fraction of FP32, so
 // the assembly of the fronts and every refinement residual read the stored
 // values instead of re-deriving them per cell (and per neighbour for A^T).
-__global__ void k_coef(OpDev o, double2 *coef) {
+// coef[d * ld + k]: ld = n for one operator, the batch's total for problem
+// b's slice of a batch (coef then points at the slice).
+__global__ void k_coef(OpDev o, double2 *coef, int64_t ld) {
     const int64_t n = (int64_t)o.Nx * o.Ny;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
         double2 c[5];
         stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
 #pragma unroll
-        for (int d = 0; d < 5; ++d) coef[d * n + k] = c[d];
+        for (int d = 0; d < 5; ++d) coef[d * ld + k] = c[d];
     }
 }
 
@@ -1633,6 +1635,8 @@ struct fdfd_factor {
     bool numeric_done = false;
     bool has_p = false;  // PML factors known: transposed solves allowed
     int Nx = 0, Ny = 0;
+    int batch = 1;   // problems of a batch symbolic (stacked grids, one forest)
+    int rows = 0;    // rows per problem
     fdfd_factor_stats stats{};
 };
 
@@ -2567,7 +2571,7 @@ int64_t factor_bytes_of(const Symbolic &S, int precision, int max_nrhs) {
     b += 4 * S.sum_m * 4 + 7 * n * 4;                    // vars, relmap, inverse maps, nbr, var maps, pivots
     b += (int64_t)(S.Nx + S.Ny) * 16;
     b += 5 * n * 16;                                     // operator coefficients
-    b += (int64_t)norms_partial_count(max_nrhs) * 8 + 4 * max_nrhs * 8 + 64;
+    b += (int64_t)norms_partial_count(max_nrhs * S.batch) * 8 + 4 * max_nrhs * S.batch * 8 + 64;
     if (precision == FDFD_PREC_C64_TC) b += tc_layout(S, nullptr, nullptr) + (int64_t)S.nf * sizeof(TcFront);
     b += bwd_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8;
     b += coop_layout(S, max_nrhs, nullptr, nullptr) * elem + (int64_t)S.nf * 8 + 16;
@@ -2630,6 +2634,9 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
     f->n = (int64_t)S.Nx * S.Ny;
     f->Nx = S.Nx;
     f->Ny = S.Ny;
+    f->batch = S.batch;
+    f->rows = S.rows;
+    const int nseg = max_nrhs * S.batch;  // norm segments: right-hand side x problem
     cudaGetDevice(&f->device);
 
     std::vector<FrontD> fd(S.nf);
@@ -2661,8 +2668,8 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
               alloc((void **)&f->d_r, n * max_nrhs * 16) && alloc((void **)&f->d_d, n * max_nrhs * 16) &&
               alloc((void **)&f->d_tmp, n * max_nrhs * 16) && alloc((void **)&f->d_isxf, S.Nx * 16) &&
               alloc((void **)&f->d_isyf, S.Ny * 16) &&
-              alloc((void **)&f->d_partial, norms_partial_count(max_nrhs) * 8) &&
-              alloc((void **)&f->d_norm, max_nrhs * 8) && alloc((void **)&f->d_sin, max_nrhs * 8) &&
+              alloc((void **)&f->d_partial, norms_partial_count(nseg) * 8) &&
+              alloc((void **)&f->d_norm, nseg * 8) && alloc((void **)&f->d_sin, max_nrhs * 8) &&
               alloc((void **)&f->d_sout, max_nrhs * 8) && alloc((void **)&f->d_unit, 8 * 8) &&
               alloc((void **)&f->d_maxdiag, 8) && alloc((void **)&f->d_tiny, 4) &&
               alloc((void **)&f->d_coef, 5 * n * 16);
@@ -2670,7 +2677,7 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         free_factor(f);
         return fail(FDFD_ERR_OOM, "factor_create: device allocation failed");
     }
-    cudaError_t e = cudaMallocHost((void **)&f->h_norm, 8 * sizeof(double));
+    cudaError_t e = cudaMallocHost((void **)&f->h_norm, std::max(8, nseg) * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&f->h_err, sizeof(int));
     for (auto &ev : f->ev)
         if (e == cudaSuccess) e = cudaEventCreate(&ev);
@@ -2809,6 +2816,7 @@ static void use_stored_coefficients(const fdfd_factor *fac, const fdfd_operator 
 
 extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, void *stream) {
     if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_numeric: NULL factor");
+    if (fac->batch > 1) return fail(FDFD_ERR_BAD_ARG, "factor_numeric: a batch factor takes fdfd_factor_numeric_batch");
     OpDev o;
     int rc = make_opdev(op, &o);
     if (rc) return rc;
@@ -2824,7 +2832,7 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
     fac->coef_valid = false;
     if (!o.stencil) {
         prof_begin(PROF_ASSEMBLE, st);
-        k_coef<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_coef);
+        k_coef<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_coef, fac->n);
         prof_end(PROF_ASSEMBLE, st, 1);
         o.stencil = fac->d_coef;
     }
@@ -2878,33 +2886,25 @@ extern "C" int fdfd_factor_set_wait_limit(fdfd_factor *fac, int64_t polls) {
     return FDFD_OK;
 }
 
-extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, const void *b, void *x,
-                                  int32_t nrhs, int32_t transpose, double tol, int32_t max_iter,
-                                  void *stream) {
-    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_refined: NULL argument");
-    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_refined: factor has no numeric values");
-    if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "solve_refined: nrhs out of range");
-    if (max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_refined: max_iter must be >= 0");
-    OpDev o;
-    int rc = make_opdev(op, &o);
-    if (rc) return rc;
-    if (op->Nx != fac->Nx || op->Ny != fac->Ny)
-        return fail(FDFD_ERR_BAD_ARG, "solve_refined: operator grid differs from the factor grid");
-    use_stored_coefficients(fac, op, &o);
-    cudaStream_t st = (cudaStream_t)stream;
+// FP64 iterative refinement shared by the single and the batch entry
+// points: x = M^-1 b, then x += M^-1 (b - A x) until every one of the nseg
+// segments (seg entries each: a right-hand side of one problem) has
+// ||b - A x|| <= tol ||b|| or max_iter steps were taken.  seg_rel (host,
+// nseg doubles, optional) receives the final relative residuals.
+static int refine_loop(fdfd_factor *fac, const OpDev &o, const double2 *bb, double2 *xx, int nrhs,
+                       int transpose, double tol, int max_iter, int64_t seg, int nseg, double *seg_rel,
+                       const char *who, cudaStream_t st) {
     const int64_t n = fac->n;
-    const double2 *bb = (const double2 *)b;
-    double2 *xx = (double2 *)x;
     CUDA_TRY(cudaEventRecord(fac->ev[2], st));
     CUDA_TRY(cudaMemsetAsync(fac->d_solve_err, 0, sizeof(int), st));
-    double bnorm[8];
+    std::vector<double> bnorm(nseg);
     prof_begin(PROF_OTHER, st);
-    rc = norms_device(bb, n, nrhs, fac->d_partial, fac->d_norm, st);
+    int rc = norms_device(bb, seg, nseg, fac->d_partial, fac->d_norm, st);
     if (rc) return rc;
     prof_end(PROF_OTHER, st, 2);
-    CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nseg * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
-    for (int r = 0; r < nrhs; ++r) bnorm[r] = fac->h_norm[r];
+    for (int r = 0; r < nseg; ++r) bnorm[r] = fac->h_norm[r];
     rc = apply_factor(fac, bb, xx, nrhs, transpose, st);
     if (rc) return rc;
     double worst = 0.0;
@@ -2914,18 +2914,19 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
         prof_begin(PROF_OTHER, st);
         rc = apply_device(o, xx, bb, fac->d_r, nrhs, transpose ? 3 : 0, st);
         if (rc) return rc;
-        rc = norms_device(fac->d_r, n, nrhs, fac->d_partial, fac->d_norm, st);
+        rc = norms_device(fac->d_r, seg, nseg, fac->d_partial, fac->d_norm, st);
         if (rc) return rc;
         prof_end(PROF_OTHER, st, 3);
-        CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(fac->h_norm, fac->d_norm, nseg * sizeof(double), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_solve_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaStreamSynchronize(st));
         if (*fac->h_err)
-            return fail(FDFD_ERR_TIMEOUT, "solve_refined: a bounded wait of the cooperative substitutions ran "
-                                          "out (the solution is not valid)");
+            return fail(FDFD_ERR_TIMEOUT, std::string(who) + ": a bounded wait of the cooperative substitutions "
+                                                              "ran out (the solution is not valid)");
         worst = 0.0;
-        for (int r = 0; r < nrhs; ++r) {
+        for (int r = 0; r < nseg; ++r) {
             const double rel = bnorm[r] > 0 ? fac->h_norm[r] / bnorm[r] : fac->h_norm[r];
+            if (seg_rel) seg_rel[r] = rel;
             worst = std::max(worst, rel);
         }
         if (!(worst > tol) || it >= max_iter) break;
@@ -2940,10 +2941,95 @@ extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, con
     fac->stats.refine_iters = it;
     fac->stats.rel_residual = worst;
     if (!(worst <= tol))
-        return fail(FDFD_ERR_NOT_CONVERGED, "solve_refined: residual " + std::to_string(worst) +
+        return fail(FDFD_ERR_NOT_CONVERGED, std::string(who) + ": residual " + std::to_string(worst) +
                                                 " above tolerance after " + std::to_string(it) +
                                                 " refinement steps");
     return FDFD_OK;
+}
+
+extern "C" int fdfd_solve_refined(fdfd_factor *fac, const fdfd_operator *op, const void *b, void *x,
+                                  int32_t nrhs, int32_t transpose, double tol, int32_t max_iter,
+                                  void *stream) {
+    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_refined: NULL argument");
+    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_refined: factor has no numeric values");
+    if (fac->batch > 1) return fail(FDFD_ERR_BAD_ARG, "solve_refined: a batch factor takes fdfd_solve_refined_batch");
+    if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "solve_refined: nrhs out of range");
+    if (max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_refined: max_iter must be >= 0");
+    OpDev o;
+    int rc = make_opdev(op, &o);
+    if (rc) return rc;
+    if (op->Nx != fac->Nx || op->Ny != fac->Ny)
+        return fail(FDFD_ERR_BAD_ARG, "solve_refined: operator grid differs from the factor grid");
+    use_stored_coefficients(fac, op, &o);
+    return refine_loop(fac, o, (const double2 *)b, (double2 *)x, nrhs, transpose, tol, max_iter, fac->n, nrhs,
+                       nullptr, "solve_refined", (cudaStream_t)stream);
+}
+
+// ---- batches: one forest factorization of `batch` same-grid operators -------
+// The operators' coefficients are evaluated into consecutive slices of the
+// factor's coefficient store; from then on the forest is one explicit-
+// stencil operator of batch * rows rows whose wrap stays inside each
+// problem's rows (OpDev::Nxp), so every level's launches cover the fronts
+// of all problems and the refinement residual of all problems is one pass.
+static OpDev batch_opdev(const fdfd_factor *fac) {
+    OpDev o{};
+    o.Nx = fac->Nx;
+    o.Ny = fac->Ny;
+    o.Nxp = fac->rows;
+    o.stencil = fac->d_coef;
+    return o;
+}
+
+extern "C" int fdfd_factor_numeric_batch(fdfd_factor *fac, const fdfd_operator *ops, int32_t count,
+                                         void *stream) {
+    if (!fac || !ops) return fail(FDFD_ERR_BAD_ARG, "factor_numeric_batch: NULL argument");
+    if (count != fac->batch)
+        return fail(FDFD_ERR_BAD_ARG, "factor_numeric_batch: count must equal the symbolic's batch (" +
+                                          std::to_string(fac->batch) + ")");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n1 = (int64_t)fac->rows * fac->Ny;
+    CUDA_TRY(cudaEventRecord(fac->ev[0], st));
+    for (int b = 0; b < count; ++b) {
+        OpDev o;
+        int rc = make_opdev(&ops[b], &o);
+        if (rc) return rc;
+        if (ops[b].Nx != fac->rows || ops[b].Ny != fac->Ny)
+            return fail(FDFD_ERR_BAD_ARG, "factor_numeric_batch: operator " + std::to_string(b) +
+                                              " differs from the batch's grid");
+        prof_begin(PROF_ASSEMBLE, st);
+        k_coef<<<grid1(n1), 256, 0, st>>>(o, fac->d_coef + b * n1, fac->n);
+        prof_end(PROF_ASSEMBLE, st, 1);
+    }
+    fac->has_p = false;
+    fac->coef_valid = false;
+    const OpDev o = batch_opdev(fac);
+    int rc = (fac->precision != FDFD_PREC_C128) ? factor_levels<c64, float>(fac, o, st)
+                                                : factor_levels<c128, double>(fac, o, st);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(fac->ev[1], st));
+    if (fac->d_tcerr) {
+        CUDA_TRY(cudaMemcpyAsync(fac->h_err, fac->d_tcerr, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (*fac->h_err) {
+            fac->numeric_done = false;
+            return fail(FDFD_ERR_TIMEOUT, "factor_numeric_batch: a bounded wait of the tensor-core Schur update "
+                                          "ran out (the factor is not valid)");
+        }
+    }
+    fac->numeric_done = true;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_solve_refined_batch(fdfd_factor *fac, const void *b, void *x, int32_t nrhs, double tol,
+                                        int32_t max_iter, double *rel_residuals, void *stream) {
+    if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_refined_batch: NULL argument");
+    if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_refined_batch: factor has no numeric values");
+    if (nrhs < 1 || nrhs > fac->max_nrhs) return fail(FDFD_ERR_BAD_ARG, "solve_refined_batch: nrhs out of range");
+    if (max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_refined_batch: max_iter must be >= 0");
+    const OpDev o = batch_opdev(fac);
+    const int64_t n1 = (int64_t)fac->rows * fac->Ny;
+    return refine_loop(fac, o, (const double2 *)b, (double2 *)x, nrhs, 0, tol, max_iter, n1, nrhs * fac->batch,
+                       rel_residuals, "solve_refined_batch", (cudaStream_t)stream);
 }
 
 // Right-preconditioned restarted GMRES in FP64 with the factor as the
@@ -2957,6 +3043,7 @@ extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const
                                 void *stream) {
     if (!fac || !b || !x) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: NULL argument");
     if (!fac->numeric_done) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: factor has no numeric values");
+    if (fac->batch > 1) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: not available for a batch factor");
     if (restart < 1 || restart > 30 || max_iter < 0) return fail(FDFD_ERR_BAD_ARG, "solve_gmres: restart must be 1..30");
     OpDev o;
     int rc = make_opdev(op, &o);

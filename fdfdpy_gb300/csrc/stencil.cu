@@ -398,6 +398,7 @@ int make_opdev(const fdfd_operator *op, OpDev *d) {
     if (!op->stencil && (!(op->xlen > 0.0) || !(op->ylen > 0.0) || !(op->L0 > 0.0)))
         return fail(FDFD_ERR_BAD_ARG, "operator: xlen, ylen and L0 must be positive");
     d->stencil = (const double2 *)op->stencil;
+    d->Nxp = 0;
     if (op->stencil) {
         d->Nx = op->Nx; d->Ny = op->Ny; d->pol = op->pol; d->averaging = 0;
         d->invdx = d->invdy = d->invmu = d->eps0L = d->w2 = d->w2mu = d->w2e0L = 0.0;

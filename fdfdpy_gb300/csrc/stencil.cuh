@@ -21,6 +21,10 @@ namespace fdfd {
 
 struct OpDev {
     int Nx, Ny, pol, averaging;
+    // rows per problem of a batch of stacked grids (explicit-stencil
+    // operators only): rows [b Nxp, (b + 1) Nxp) wrap among themselves;
+    // 0 = one problem
+    int Nxp;
     double invdx, invdy;  // 1/dx, 1/dy with dx = xlen/Nx (linalg.py:25-33)
     double invmu;         // 1/(MU_0*L0)
     double eps0L;         // EPSILON_0*L0
@@ -126,6 +130,11 @@ __device__ inline void stencil_row(const OpDev &o, int i, int j, double2 c[5]) {
 // Neighbour cell index in direction d (0 xm, 1 xp, 2 ym, 3 yp) and the
 // direction that points back.
 __device__ __forceinline__ int nbr_cell(const OpDev &o, int i, int j, int d) {
+    if (o.Nxp && d < 2) {
+        const int i0 = i - i % o.Nxp;
+        if (d == 0) return ((i == i0) ? i0 + o.Nxp - 1 : i - 1) * o.Ny + j;
+        return ((i == i0 + o.Nxp - 1) ? i0 : i + 1) * o.Ny + j;
+    }
     switch (d) {
         case 0: return ((i == 0) ? o.Nx - 1 : i - 1) * o.Ny + j;
         case 1: return ((i == o.Nx - 1) ? 0 : i + 1) * o.Ny + j;

@@ -222,6 +222,90 @@ int build_symbolic(int32_t Nx, int32_t Ny, int32_t leaf_area, Symbolic &S) {
     }
     for (int32_t s = 0; s < n; ++s)
         if (S.var_front[s] < 0) return fail(FDFD_ERR_BAD_ARG, "symbolic: variable never eliminated");
+    S.rows = Nx;
+    return FDFD_OK;
+}
+
+// The forest of `batch` copies of one tree.  Copy b of front f of level L
+// gets the id level_ptr'[L] + b * cnt_L + (f - level_ptr[L]) (a level's
+// copies are contiguous, so one launch per level still covers every front
+// of every problem); copy b's variables are the single tree's plus b * n.
+int replicate_symbolic(const Symbolic &S1, int32_t batch, Symbolic &S) {
+    if (batch < 1) return fail(FDFD_ERR_BAD_ARG, "symbolic: batch must be >= 1");
+    const int64_t n1 = (int64_t)S1.Nx * S1.Ny;
+    if (n1 * batch > ((int64_t)1 << 30) / 5 || S1.sum_m * batch > INT32_MAX)
+        return fail(FDFD_ERR_BAD_ARG, "symbolic: batch too large for int32 indices");
+    const int32_t nf1 = S1.nf, nlev = S1.nlev;
+    S = Symbolic();
+    S.batch = batch;
+    S.rows = S1.Nx;
+    S.Nx = S1.Nx * batch;
+    S.Ny = S1.Ny;
+    S.leaf_area = S1.leaf_area;
+    S.nf = nf1 * batch;
+    S.nlev = nlev;
+    S.level_ptr.assign(nlev + 1, 0);
+    for (int32_t L = 0; L < nlev; ++L)
+        S.level_ptr[L + 1] = S.level_ptr[L] + batch * (S1.level_ptr[L + 1] - S1.level_ptr[L]);
+    auto nid = [&](int32_t b, int32_t f) -> int32_t {
+        if (f < 0) return -1;
+        const int32_t L = S1.height[f], cnt = S1.level_ptr[L + 1] - S1.level_ptr[L];
+        return S.level_ptr[L] + b * cnt + (f - S1.level_ptr[L]);
+    };
+    const int32_t nf = S.nf;
+    S.p.resize(nf); S.m.resize(nf); S.ld.resize(nf); S.parent.resize(nf);
+    S.child0.resize(nf); S.child1.resize(nf); S.height.resize(nf);
+    S.vars_off.resize(nf); S.pool_off.resize(nf);
+    std::vector<int32_t> src(nf), prob(nf);
+    for (int32_t b = 0; b < batch; ++b)
+        for (int32_t f = 0; f < nf1; ++f) {
+            const int32_t g = nid(b, f);
+            src[g] = f;
+            prob[g] = b;
+            S.p[g] = S1.p[f]; S.m[g] = S1.m[f]; S.ld[g] = S1.ld[f]; S.height[g] = S1.height[f];
+            S.parent[g] = nid(b, S1.parent[f]);
+            S.child0[g] = nid(b, S1.child0[f]);
+            S.child1[g] = nid(b, S1.child1[f]);
+        }
+    int64_t off = 0, poff = 0;
+    for (int32_t g = 0; g < nf; ++g) {
+        S.vars_off[g] = (int32_t)off;
+        S.pool_off[g] = poff;
+        off += S.m[g];
+        poff += (int64_t)S.ld[g] * S.m[g];
+    }
+    S.sum_m = off;
+    S.pool_entries = poff;
+    S.vars.resize(off);
+    S.relmap.resize(off);
+    for (int32_t g = 0; g < nf; ++g) {
+        const int32_t f = src[g], m = S.m[g];
+        const int32_t add = (int32_t)(prob[g] * n1);
+        const int32_t *v1 = S1.vars.data() + S1.vars_off[f];
+        const int32_t *r1 = S1.relmap.data() + S1.vars_off[f];
+        int32_t *v = S.vars.data() + S.vars_off[g];
+        int32_t *r = S.relmap.data() + S.vars_off[g];
+        for (int32_t k = 0; k < m; ++k) {
+            v[k] = v1[k] + add;
+            r[k] = r1[k];
+        }
+    }
+    const int64_t n = n1 * batch;
+    S.var_front.resize(n);
+    S.var_loc.resize(n);
+    S.nbr_loc.resize((size_t)4 * n);
+    for (int32_t b = 0; b < batch; ++b)
+        for (int64_t s = 0; s < n1; ++s) {
+            S.var_front[b * n1 + s] = nid(b, S1.var_front[s]);
+            S.var_loc[b * n1 + s] = S1.var_loc[s];
+            for (int d = 0; d < 4; ++d) S.nbr_loc[(size_t)4 * (b * n1 + s) + d] = S1.nbr_loc[(size_t)4 * s + d];
+        }
+    S.lev_max_m = S1.lev_max_m;
+    S.lev_max_p = S1.lev_max_p;
+    S.factor_entries = S1.factor_entries * batch;
+    S.factor_flops = S1.factor_flops * batch;
+    S.max_m = S1.max_m;
+    S.max_p = S1.max_p;
     return FDFD_OK;
 }
 
@@ -242,6 +326,26 @@ extern "C" int fdfd_symbolic_create(int32_t Nx, int32_t Ny, int32_t leaf_area,
     } catch (const std::bad_alloc &) {
         delete h;
         return fail(FDFD_ERR_OOM, "symbolic_create: host allocation failed");
+    }
+    *out = h;
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_symbolic_create_batch(int32_t Nx, int32_t Ny, int32_t leaf_area, int32_t batch,
+                                          fdfd_symbolic **out) {
+    if (!out) return fail(FDFD_ERR_BAD_ARG, "symbolic_create_batch: out is NULL");
+    *out = nullptr;
+    fdfd_symbolic *h = nullptr;
+    try {
+        fdfd::Symbolic one;
+        int st = fdfd::build_symbolic(Nx, Ny, leaf_area, one);
+        if (st != FDFD_OK) return st;
+        h = new fdfd_symbolic();
+        st = fdfd::replicate_symbolic(one, batch, h->s);
+        if (st != FDFD_OK) { delete h; return st; }
+    } catch (const std::bad_alloc &) {
+        delete h;
+        return fail(FDFD_ERR_OOM, "symbolic_create_batch: host allocation failed");
     }
     *out = h;
     return FDFD_OK;

@@ -205,13 +205,18 @@ def norms(v: torch.Tensor, n: int):
 
 
 class Symbolic:
-    """Nested-dissection front tree of an Nx x Ny periodic grid (host)."""
+    """Nested-dissection front tree of an Nx x Ny periodic grid (host); with
+    batch > 1 the forest of `batch` copies (one factorization of `batch`
+    operators of that grid)."""
 
-    def __init__(self, Nx, Ny, leaf_area=DEFAULT_LEAF_AREA):
+    def __init__(self, Nx, Ny, leaf_area=DEFAULT_LEAF_AREA, batch=1):
         h = C.c_void_p()
-        N.call("fdfd_symbolic_create", int(Nx), int(Ny), int(leaf_area), C.byref(h))
+        if batch > 1:
+            N.call("fdfd_symbolic_create_batch", int(Nx), int(Ny), int(leaf_area), int(batch), C.byref(h))
+        else:
+            N.call("fdfd_symbolic_create", int(Nx), int(Ny), int(leaf_area), C.byref(h))
         self.handle = h
-        self.Nx, self.Ny, self.leaf_area = int(Nx), int(Ny), int(leaf_area)
+        self.Nx, self.Ny, self.leaf_area, self.batch = int(Nx), int(Ny), int(leaf_area), int(batch)
         info = N.SymbolicInfo()
         N.call("fdfd_symbolic_info_get", h, C.byref(info))
         self.info = info
@@ -234,13 +239,14 @@ _sym_cache: dict = {}
 _sym_lock = threading.Lock()
 
 
-def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA) -> Symbolic:
-    """Symbolic analyses are cached per grid shape (they depend on nothing else)."""
-    key = (int(Nx), int(Ny), int(leaf_area))
+def symbolic_for(Nx, Ny, leaf_area=DEFAULT_LEAF_AREA, batch=1) -> Symbolic:
+    """Symbolic analyses are cached per grid shape and batch size (they
+    depend on nothing else)."""
+    key = (int(Nx), int(Ny), int(leaf_area)) + ((int(batch),) if batch > 1 else ())
     with _sym_lock:
         s = _sym_cache.get(key)
         if s is None:
-            s = Symbolic(*key)
+            s = Symbolic(*key[:3], batch=int(batch))
             _sym_cache[key] = s
         return s
 
@@ -275,8 +281,9 @@ class Factor:
             raise ValueError("precision must be 'c128', 'c64' or 'c64tc'")
         device()
         self.sym, self.precision, self.max_nrhs = sym, precision, int(max_nrhs)
-        shared = _sym_cache.get((sym.Nx, sym.Ny, sym.leaf_area)) is sym
-        self._key = (sym.Nx, sym.Ny, sym.leaf_area, precision, self.max_nrhs) if shared else None
+        skey = (sym.Nx, sym.Ny, sym.leaf_area) + ((sym.batch,) if sym.batch > 1 else ())
+        shared = _sym_cache.get(skey) is sym
+        self._key = skey + (precision, self.max_nrhs) if shared else None
         h = None
         self._events = {}
         if self._key is not None:
@@ -399,6 +406,58 @@ class Factor:
                     N.lib().fdfd_factor_destroy(h)
         except Exception:
             pass
+
+
+class BatchFactor(Factor):
+    """One forest factorization of `batch` operators of the same grid,
+    polarization and frequency (fdfd_factor_numeric_batch): every level's
+    launches cover the fronts of all of them."""
+
+    def __init__(self, sym: Symbolic, precision="c64", max_nrhs=8, pivot_tol=None, fused_max_m=None):
+        if sym.batch < 2:
+            raise ValueError("BatchFactor needs a batch symbolic (symbolic_for(..., batch=B), B >= 2)")
+        super().__init__(sym, precision, max_nrhs, pivot_tol, fused_max_m)
+        self.batch = sym.batch
+        self.ops = None
+
+    def numeric(self, ops):
+        if len(ops) != self.batch:
+            raise ValueError(f"BatchFactor.numeric: {len(ops)} operators for a batch of {self.batch}")
+        structs = (N.Operator * self.batch)(*[o.struct() for o in ops])
+        N.call("fdfd_factor_numeric_batch", self.handle, structs, self.batch, stream_ptr())
+        self._used()
+        self.ops = list(ops)   # their buffers are read by the queued coefficient kernels
+        self.op = None
+        return self
+
+    def solve_batch(self, rhs, tol=1e-10, max_iter=30, raise_on_fail=False):
+        """rhs: list of `batch` device or host arrays (nrhs_b, n) (nrhs_b <= 8;
+        None or 0 rows for a problem with nothing to solve).  Returns (list
+        of (nrhs_b, n) complex128 device tensors, list of per-problem worst
+        relative residuals)."""
+        n = self.sym.Nx * self.sym.Ny
+        blocks = [None if r is None else as_c128(r).reshape(-1, n) for r in rhs]
+        nr = max([b.shape[0] for b in blocks if b is not None] + [1])
+        if nr > self.max_nrhs:
+            raise ValueError(f"at most {self.max_nrhs} right-hand sides per problem")
+        B = torch.zeros((nr, self.batch, n), dtype=torch.complex128, device=device())
+        for p, blk in enumerate(blocks):
+            if blk is not None and blk.shape[0]:
+                B[:blk.shape[0], p] = blk
+        X = torch.empty_like(B)
+        rel = (C.c_double * (nr * self.batch))()
+        code = N.lib().fdfd_solve_refined_batch(self.handle, _ptr(B), _ptr(X), nr, float(tol), int(max_iter), rel,
+                                                stream_ptr())
+        if code != N.FDFD_ERR_NOT_CONVERGED or raise_on_fail:
+            N.check(code, "fdfd_solve_refined_batch")
+        self._used()
+        rr = np.array(rel[:]).reshape(nr, self.batch)
+        xs, worst = [], []
+        for p, blk in enumerate(blocks):
+            k = 0 if blk is None else blk.shape[0]
+            xs.append(X[:k, p].contiguous())
+            worst.append(float(rr[:k, p].max()) if k else 0.0)
+        return xs, worst
 
 
 class StencilOperator:

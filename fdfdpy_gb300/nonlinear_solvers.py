@@ -180,9 +180,13 @@ def _rel_change(E, Eprev):
 
 
 def newton_device(op_lin, b, kerr, E0, precision, conv_threshold=1e-10, max_num_iter=50, lin_tol=1e-11,
-                  reuse_factor=True, max_inner=60, stats=None):
+                  reuse_factor=True, max_inner=30, stats=None):
     """Newton iterations from the device field E0; returns (E, conv_array,
-    factor) with the factor last used (of J11 at some iterate)."""
+    factor) with the factor last used (of J11 at some iterate).  The factor
+    is reused while it keeps preconditioning well: an iteration whose reuse
+    attempt ran out of inner iterations refactors, and so does the next one
+    (the iterate is moving fast) until an iteration converges with the
+    factor in at most max_inner / 2 applications."""
     sym = engine.symbolic_for(op_lin.Nx, op_lin.Ny)
     conv_array = np.zeros((max_num_iter, 1))
     E = E0
@@ -190,17 +194,23 @@ def newton_device(op_lin, b, kerr, E0, precision, conv_threshold=1e-10, max_num_
     stats = {} if stats is None else stats
     stats.update(factorizations=0, inner=[], linear_rel_residual=[])
     convergence = float('inf')
+    trust = False        # the factor in hand preconditioned the last solve well
     for istep in range(max_num_iter):
         Eprev = E
         fx, J11, J12 = _f_and_jac(op_lin, b, kerr, Eprev)
         rel, its, d = 1.0, 0, None
-        if fac is not None and reuse_factor:
+        if fac is not None and reuse_factor and trust:
             d, rel, its = solve_complex2real(fac, J11, J12, fx, tol=lin_tol, max_iter=max_inner)
         if d is None or rel > max(lin_tol, 1e-9):
+            reuse_failed = d is not None
             fac = engine.Factor(sym, precision).numeric(J11)
             stats['factorizations'] += 1
             d, rel, its2 = solve_complex2real(fac, J11, J12, fx, tol=lin_tol)
             its += its2
+            # after a failed reuse the iterate is moving fast: refactor next time too
+            trust = not reuse_failed and its2 <= max_inner // 2
+        else:
+            trust = its <= max_inner // 2
         stats['inner'].append(its)
         stats['linear_rel_residual'].append(rel)
         E = Eprev - d

@@ -9,6 +9,12 @@ Each precision first runs once outside the ranges (warm-up: module load,
 first-touch of the factor memory), then once inside `factor_<precision>`
 and `solve_<precision>`.  The workload is the benchmark's: Hz, dl = 0.01,
 NPML = [20, 20], eps in 16 x 16-cell blocks from {1, 12.25}, line source.
+
+With --stencil the factorization is skipped and the grid's stencil passes
+run instead, each once for warm-up and once inside the range `stencil`:
+CSR assembly (K1), the FP64 residual (K2), field recovery (K8), the
+adjoint gradient (K9, Hz), the Kerr terms (K1-NL) and the flux probe -- the
+HBM-bound kernels, for a capture of their DRAM counters.
 """
 from __future__ import annotations
 
@@ -38,11 +44,15 @@ def main(argv=None):
     ap.add_argument("--fused-max-m", type=int, default=None,
                     help="largest front factored in one launch per level (-1: the default; 0: never)")
     ap.add_argument("--repeat", type=int, default=1, help="timed factorizations outside the ranges")
+    ap.add_argument("--stencil", action="store_true", help="the stencil passes instead of factor + solve")
     args = ap.parse_args(argv)
     N = args.size
     eps, src = workload(N)
     om = 2 * np.pi * C_0 / 1.55e-6
     op = engine.DeviceOperator(om, eps, N * 0.01, N * 0.01, [20, 20], "Hz", 1e-6)
+    if args.stencil:
+        stencil_passes(op, N, om)
+        return
     b = engine.as_c128(1j * om * src).reshape(1, -1).repeat(args.nrhs, 1)
     sym = engine.symbolic_for(N, N) if args.leaf is None else engine.Symbolic(N, N, args.leaf)
     for prec in args.precision:
@@ -67,6 +77,34 @@ def main(argv=None):
         print(f"{prec}: factor {best:.1f} ms, solve {st['solve_ms']:.2f} ms, "
               f"tiny pivots {st['tiny_pivots']}", flush=True)
         del fac
+
+
+def stencil_passes(op, N, om):
+    from . import _native as NAT
+    from .nonlinearity import Nonlinearity
+    from .nonlinear_solvers import KerrTerms
+    g = torch.Generator(device="cpu").manual_seed(0)
+    x = (torch.randn(N * N, generator=g, dtype=torch.float64) + 1j * torch.randn(N * N, generator=g,
+                                                                                  dtype=torch.float64)).cuda()
+    region = np.zeros((N, N))
+    region[N // 4:3 * N // 4, N // 4:3 * N // 4] = 1
+    kerr = KerrTerms(om, 1e-6, op.eps, [Nonlinearity(2.8e-6, region)])
+    flux = torch.empty((), dtype=torch.float64, device="cuda")
+
+    def run():
+        op.csr_device()
+        op.residual(x, x)
+        op.fields(x)
+        op.grad_eps(x, x)
+        kerr(x, eps_nl=True, jac=True)
+        NAT.call("fdfd_flux_probe", N, N, 1, 0, N // 2, 0, N - 1, 0.01, engine._ptr(x), engine._ptr(x),
+                 engine._ptr(flux), engine.stream_ptr())
+    run()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("stencil")
+    run()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
 
 
 if __name__ == "__main__":

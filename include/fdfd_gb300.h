@@ -234,6 +234,14 @@ typedef struct fdfd_symbolic_info {
 
 int fdfd_symbolic_create(int32_t Nx, int32_t Ny, int32_t leaf_area,
                          fdfd_symbolic **out);
+/* A batch symbolic: `batch` copies of the Nx x Ny front tree as one forest,
+ * for factoring `batch` operators of the same grid in one pass (every
+ * level's launches cover the fronts of all of them).  Problem b's unknowns
+ * are [b n, (b + 1) n), n = Nx Ny; vectors are the problems' vectors one
+ * after the other, and the info's Nx is batch * Nx.  No counterpart in
+ * fdfdpy (it serves many independent solver_direct calls at once). */
+int fdfd_symbolic_create_batch(int32_t Nx, int32_t Ny, int32_t leaf_area,
+                               int32_t batch, fdfd_symbolic **out);
 int fdfd_symbolic_info_get(const fdfd_symbolic *sym, fdfd_symbolic_info *info);
 /* Copies one host array out (tests and diagnostics).  which:
  *  0 front p (n_fronts int32)     1 front m          2 front parent
@@ -307,6 +315,25 @@ int fdfd_factor_set_pivot_tol(fdfd_factor *fac, double rel_tol);
  * Takes effect at the next fdfd_factor_numeric.  No counterpart in
  * fdfdpy.                                                                */
 int fdfd_factor_set_fused_limit(fdfd_factor *fac, int32_t max_m);
+/* Batch factors (a factor created on a batch symbolic): factor `count` =
+ * batch operators of the symbolic's grid (ops[b] for problem b) in one
+ * forest factorization.  The batch shares one scaling and one static-pivot
+ * threshold (relative to the largest diagonal entry of the batch), so it is
+ * meant for operators of the same grid, polarization and frequency that
+ * differ in eps_r.  The coefficients are evaluated at this call; the
+ * operators' buffers are not read afterwards.                           */
+int fdfd_factor_numeric_batch(fdfd_factor *fac, const fdfd_operator *ops,
+                              int32_t count, void *stream);
+/* FP64 iterative refinement of the batch: b and x hold nrhs columns of
+ * batch * n entries (column r, problem p at offset (r batch + p) n); every
+ * (column, problem) segment is refined until its ||b - A x|| <= tol ||b||
+ * against the factored operators (FDFD_ERR_NOT_CONVERGED otherwise, x
+ * still written).  rel_residuals (host, nrhs * batch doubles, optional)
+ * receives the final relative residual of segment r batch + p; a zero
+ * segment (a problem with fewer right-hand sides) stays zero.           */
+int fdfd_solve_refined_batch(fdfd_factor *fac, const void *b, void *x,
+                             int32_t nrhs, double tol, int32_t max_iter,
+                             double *rel_residuals, void *stream);
 /* Polls a bounded wait of the cooperative substitutions (grid barrier,
  * published panel values) makes before it gives up and the call returns
  * FDFD_ERR_TIMEOUT; -1 restores the built-in limits (2^24 barrier polls,

@@ -1,7 +1,9 @@
 """The continuous-batching solve server: each result is the same alone and
-in the mix (bitwise: every request's arithmetic is independent of the
-others'), cached factors are reused, admission respects the memory
-budget, and every result meets its residual tolerance."""
+in the mix (bitwise without batch factorizations -- every request's
+arithmetic is then independent of the others' -- and within the mixed-
+precision field bar, 1e-8 relative, when requests of one grid share a
+forest factorization), cached factors are reused, admission respects the
+memory budget, and every result meets its residual tolerance."""
 import numpy as np
 import pytest
 
@@ -24,15 +26,18 @@ def test_alone_equals_mix_and_meets_tolerance():
         s = srv.run([r], realtime=False)
         assert s["failed"] == 0
         alone[r.rid] = r.x
-    mix = _requests()
-    srv = SolveServer(slots=4, precision="c64", tol=1e-10)
-    s = srv.run(mix, realtime=False)
-    assert s["failed"] == 0, [r.error for r in mix if r.error]
-    assert s["solves"] == sum(r.nrhs for r in mix)
-    assert s["max_rel_residual"] <= 1e-10
-    for r in mix:
-        a = alone[r.rid]
-        assert np.linalg.norm(r.x - a) <= 1e-12 * np.linalg.norm(a), r.rid
+    for batch_max, bar in ((1, 1e-12), (4, 1e-8)):
+        mix = _requests()
+        srv = SolveServer(slots=4, precision="c64", tol=1e-10, batch_max=batch_max)
+        s = srv.run(mix, realtime=False)
+        assert s["failed"] == 0, [r.error for r in mix if r.error]
+        assert s["solves"] == sum(r.nrhs for r in mix)
+        assert s["max_rel_residual"] <= 1e-10
+        if batch_max > 1:
+            assert s["batched_requests"] > 0 and s["factorizations"] < len(mix) - s["cache_hits"]
+        for r in mix:
+            a = alone[r.rid]
+            assert np.linalg.norm(r.x - a) <= bar * np.linalg.norm(a), (batch_max, r.rid)
 
 
 def test_results_match_oracle():
@@ -113,9 +118,56 @@ def test_tensor_core_requests_alone_equal_mix():
         assert s["failed"] == 0, r.error
         alone[r.rid] = r.x
     mix = reqs()
-    s = SolveServer(slots=3, precision="c64tc", tol=1e-10).run(mix, realtime=False)
+    s = SolveServer(slots=3, precision="c64tc", tol=1e-10, batch_max=1).run(mix, realtime=False)
     assert s["failed"] == 0, [r.error for r in mix if r.error]
     assert s["max_rel_residual"] <= 1e-10
     for r in mix:
         a = alone[r.rid]
         assert np.linalg.norm(r.x - a) <= 1e-12 * np.linalg.norm(a), r.rid
+
+
+def test_batch_factor_matches_single_factors():
+    """A forest factorization of several operators of one grid (every
+    level's front updates of all of them in one launch) against the same
+    operators factored one by one and against the oracle: residual <= 1e-10
+    per (problem, right-hand side), fields within 1e-8; a problem with no
+    right-hand sides stays zero; a cached batch entry serves a later hit."""
+    import torch
+    from oracle import fdfd_oracle as O
+    from fdfdpy_gb300 import engine
+    rng = np.random.default_rng(12)
+    N, B = 96, 3
+    om = 2 * np.pi * O.C_0 / 1.55e-6
+    for pol, prec in (("Hz", "c64tc"), ("Ez", "c64"), ("Hz", "c128")):
+        eps = [np.kron(rng.choice([1.0, 12.25], size=(N // 8, N // 8)), np.ones((8, 8))) for _ in range(B)]
+        ops = [engine.DeviceOperator(om, e, N * 0.02, N * 0.02, [10, 10], pol, 1e-6) for e in eps]
+        fac = engine.BatchFactor(engine.symbolic_for(N, N, batch=B), prec).numeric(ops)
+        rhs = [rng.standard_normal((k, N * N)) + 1j * rng.standard_normal((k, N * N)) for k in (2, 5, 0)]
+        xs, worst = fac.solve_batch(rhs, tol=1e-10, max_iter=40)
+        assert max(worst) <= 1e-10 and worst[2] == 0.0 and xs[2].shape[0] == 0
+        for p in range(2):
+            single = engine.Factor(engine.symbolic_for(N, N), prec, max_nrhs=8).numeric(ops[p]).solve(
+                engine.as_c128(rhs[p]), tol=1e-10, max_iter=40).cpu().numpy()
+            got = xs[p].cpu().numpy()
+            A = O.construct_A(om, N * 0.02, N * 0.02, eps[p], [10, 10], pol, 1e-6)
+            for k in range(rhs[p].shape[0]):
+                assert np.linalg.norm(A @ got[k] - rhs[p][k]) <= 1.01e-10 * np.linalg.norm(rhs[p][k])
+                assert np.linalg.norm(got[k] - single[k]) <= 1e-8 * np.linalg.norm(single[k])
+
+
+def test_autotuner_picks_a_measured_candidate(tmp_path):
+    """The project's autotuner times every (batch size, whole-front limit)
+    candidate on the device, keeps the fastest, writes its table, and the
+    server uses it (results still meet the tolerance)."""
+    from fdfdpy_gb300.autotune import Autotuner
+    from fdfdpy_gb300.serving import SolveServer, make_stream
+    path = tmp_path / "tune.json"
+    tuner = Autotuner(batches=(1, 2, 4), fused_limits=(-1, 0), nrhs=2, path=str(path))
+    cfg = tuner.config_for((96, 96), "c64")
+    cands = cfg["candidates"]
+    assert len(cands) == 6 and all(c["ms"] > 0 for c in cands)
+    assert cfg["solves_per_s"] == max(c["solves_per_s"] for c in cands)
+    assert Autotuner(path=str(path)).batch_for((96, 96), "c64") == cfg["batch"]
+    reqs = make_stream(n_requests=8, rate=1e6, sides=(96,), reuse=0.0, seed=4, npml=(8, 8))
+    s = SolveServer(slots=2, precision="c64", autotune=tuner, batch_max=8).run(reqs, realtime=False)
+    assert s["failed"] == 0 and s["max_rel_residual"] <= 1e-10
