@@ -416,7 +416,11 @@ def run_serving(args):
     """Serving stream with Poisson arrivals at --rate (offered load)."""
     import torch
     from fdfdpy_gb300.serving import SolveServer, make_stream
-    reqs = make_stream(n_requests=args.requests, rate=args.rate, seed=0, npml=(10, 10), block=8)
+    reqs = make_stream(n_requests=args.requests, rate=args.rate if args.rate > 0 else 1.0, seed=0, npml=(10, 10),
+                       block=8)
+    if args.rate <= 0:
+        for r in reqs:
+            r.arrival = 0.0          # closed loop: every request queued at the start
     warm = make_stream(n_requests=4, rate=1e6, seed=1, sides=(128, 256), npml=(10, 10), block=8)
     from fdfdpy_gb300.autotune import Autotuner
     tuner = Autotuner() if args.batch_max > 1 else None

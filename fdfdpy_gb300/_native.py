@@ -102,6 +102,7 @@ SIGNATURES = {
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
     "fdfd_factor_set_fused_limit": (C.c_int, [P, I32]),
     "fdfd_factor_set_wait_limit": (C.c_int, [P, I64]),
+    "fdfd_factor_set_graphs": (C.c_int, [P, I32]),
     "fdfd_factor_destroy": (None, [P]),
     "fdfd_profile_enable": (C.c_int, [I32]),
     "fdfd_profile_reset": (C.c_int, []),

@@ -1637,6 +1637,14 @@ struct fdfd_factor {
     int Nx = 0, Ny = 0;
     int batch = 1;   // problems of a batch symbolic (stacked grids, one forest)
     int rows = 0;    // rows per problem
+    // the factorization's launch sequence as a CUDA graph (captured at the
+    // first factorization, replayed by the later ones: every pointer in it
+    // is the factor's own), with the settings it was captured under
+    bool use_graphs = true;
+    cudaGraphExec_t graph = nullptr;
+    double graph_pivot_tol = 0.0;
+    int graph_fused = 0;
+    long long graph_launches[PROF_NCLASS] = {};
     fdfd_factor_stats stats{};
 };
 
@@ -1803,6 +1811,55 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
         }
     }
     CUDA_TRY(cudaGetLastError());
+    return FDFD_OK;
+}
+
+// The factorization from the coefficient store through the last level as a
+// CUDA graph.  Everything the sequence touches belongs to the factor (pool,
+// index lists, coefficient store, scratch, the look-ahead stream's events),
+// so the graph captured at the first call is replayed by every later one;
+// only the coefficient evaluation (k_coef, which reads the caller's
+// operator buffers) runs outside it.  A graph is not used while per-class
+// profiling is on (replays are not timed per class), for an explicit-
+// stencil operator read in place, or once a capture has failed.
+template <typename T, typename R>
+int factor_levels_graphed(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
+    if (!fac->use_graphs || prof_enabled() || o.stencil != fac->d_coef) return factor_levels<T, R>(fac, o, st);
+    if (fac->graph && fac->graph_pivot_tol == fac->pivot_tol && fac->graph_fused == fac->fused_max_m) {
+        CUDA_TRY(cudaGraphLaunch(fac->graph, st));
+        for (int c = 0; c < PROF_NCLASS; ++c) prof_count(c, fac->graph_launches[c]);
+        return FDFD_OK;
+    }
+    if (fac->graph) {
+        cudaGraphExecDestroy(fac->graph);
+        fac->graph = nullptr;
+    }
+    // the captured sequence sees only the scalars and the factor's own store
+    OpDev og{};
+    og.Nx = o.Nx;
+    og.Ny = o.Ny;
+    og.Nxp = o.Nxp;
+    og.pol = o.pol;
+    og.stencil = fac->d_coef;
+    long long before[PROF_NCLASS];
+    for (int c = 0; c < PROF_NCLASS; ++c) before[c] = prof_launches(c);
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int rc = factor_levels<T, R>(fac, og, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc == FDFD_OK && e == cudaSuccess) e = cudaGraphInstantiate(&fac->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (rc != FDFD_OK || e != cudaSuccess) {
+        // not capturable here: launch directly from now on
+        cudaGetLastError();
+        fac->graph = nullptr;
+        fac->use_graphs = false;
+        return factor_levels<T, R>(fac, o, st);
+    }
+    for (int c = 0; c < PROF_NCLASS; ++c) fac->graph_launches[c] = prof_launches(c) - before[c];
+    fac->graph_pivot_tol = fac->pivot_tol;
+    fac->graph_fused = fac->fused_max_m;
+    CUDA_TRY(cudaGraphLaunch(fac->graph, st));
     return FDFD_OK;
 }
 
@@ -2423,6 +2480,7 @@ int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, in
 }
 
 void free_factor(fdfd_factor *f) {
+    if (f && f->graph) cudaGraphExecDestroy(f->graph);
     if (!f) return;
     void *ptrs[] = {f->d_inv, f->d_piv, f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,
@@ -2836,8 +2894,8 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
         prof_end(PROF_ASSEMBLE, st, 1);
         o.stencil = fac->d_coef;
     }
-    rc = (fac->precision != FDFD_PREC_C128) ? factor_levels<c64, float>(fac, o, st)
-                                            : factor_levels<c128, double>(fac, o, st);
+    rc = (fac->precision != FDFD_PREC_C128) ? factor_levels_graphed<c64, float>(fac, o, st)
+                                            : factor_levels_graphed<c128, double>(fac, o, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[1], st));
     fac->coef_op = *op;
@@ -2875,6 +2933,16 @@ extern "C" int fdfd_factor_solve(fdfd_factor *fac, const void *b, void *x, int32
     if (*fac->h_err)
         return fail(FDFD_ERR_TIMEOUT, "factor_solve: a bounded wait of the cooperative substitutions ran out (the "
                                       "solution is not valid)");
+    return FDFD_OK;
+}
+
+extern "C" int fdfd_factor_set_graphs(fdfd_factor *fac, int32_t on) {
+    if (!fac) return fail(FDFD_ERR_BAD_ARG, "factor_set_graphs: NULL factor");
+    fac->use_graphs = on != 0;
+    if (!fac->use_graphs && fac->graph) {
+        cudaGraphExecDestroy(fac->graph);
+        fac->graph = nullptr;
+    }
     return FDFD_OK;
 }
 
@@ -3003,8 +3071,8 @@ extern "C" int fdfd_factor_numeric_batch(fdfd_factor *fac, const fdfd_operator *
     fac->has_p = false;
     fac->coef_valid = false;
     const OpDev o = batch_opdev(fac);
-    int rc = (fac->precision != FDFD_PREC_C128) ? factor_levels<c64, float>(fac, o, st)
-                                                : factor_levels<c128, double>(fac, o, st);
+    int rc = (fac->precision != FDFD_PREC_C128) ? factor_levels_graphed<c64, float>(fac, o, st)
+                                                : factor_levels_graphed<c128, double>(fac, o, st);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(fac->ev[1], st));
     if (fac->d_tcerr) {

@@ -43,6 +43,10 @@ void prof_begin(int cls, cudaStream_t st) {
     g_open[cls] = e;
 }
 
+bool prof_enabled() { return g_enabled; }
+long long prof_launches(int cls) { return g_launches[cls]; }
+void prof_count(int cls, long long launches) { g_launches[cls] += launches; }
+
 void prof_end(int cls, cudaStream_t st, int launches) {
     g_launches[cls] += launches;
     if (!g_enabled) return;

@@ -22,5 +22,11 @@ enum ProfClass {
 
 void prof_begin(int cls, cudaStream_t st);
 void prof_end(int cls, cudaStream_t st, int launches);
+// Whether event timing is on (graph replays are not timed per class), the
+// launch counter of a class, and a count added for the launches of a
+// replayed graph.
+bool prof_enabled();
+long long prof_launches(int cls);
+void prof_count(int cls, long long launches);
 
 }  // namespace fdfd

@@ -301,7 +301,13 @@ class Factor:
         N.call("fdfd_factor_set_pivot_tol", h, -1.0 if pivot_tol is None else float(pivot_tol))
         N.call("fdfd_factor_set_fused_limit", h, -1 if fused_max_m is None else int(fused_max_m))
         N.call("fdfd_factor_set_wait_limit", h, -1)
+        N.call("fdfd_factor_set_graphs", h, 1)
         self.op = None
+
+    def set_graphs(self, on=True):
+        """Replay the factorization as a CUDA graph (default) or launch it
+        directly."""
+        N.call("fdfd_factor_set_graphs", self.handle, int(bool(on)))
 
     def set_wait_limit(self, polls=None):
         """Polls a bounded wait of the cooperative substitutions makes before

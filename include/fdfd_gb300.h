@@ -334,6 +334,14 @@ int fdfd_factor_numeric_batch(fdfd_factor *fac, const fdfd_operator *ops,
 int fdfd_solve_refined_batch(fdfd_factor *fac, const void *b, void *x,
                              int32_t nrhs, double tol, int32_t max_iter,
                              double *rel_residuals, void *stream);
+/* on != 0 (default): the factorization's launch sequence is captured as a
+ * CUDA graph at the first fdfd_factor_numeric(_batch) of this factor and
+ * replayed by the later ones (only the evaluation of the operator's
+ * coefficients runs outside it), which takes the host's launch overhead
+ * off small grids.  Not used while kernel-class profiling is enabled or for
+ * an explicit-stencil operator.  on = 0: direct launches.  No counterpart
+ * in fdfdpy.                                                             */
+int fdfd_factor_set_graphs(fdfd_factor *fac, int32_t on);
 /* Polls a bounded wait of the cooperative substitutions (grid barrier,
  * published panel values) makes before it gives up and the call returns
  * FDFD_ERR_TIMEOUT; -1 restores the built-in limits (2^24 barrier polls,
