@@ -164,7 +164,9 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 }
 
 // ---- the GEMM ------------------------------------------------------------------
-// One CTA = one 128-row tile of C and up to kColTilesPerCta 32-column tiles,
+// One CTA = one 128-row tile of C and a run of up to kColTilesPerCta 32-column
+// tiles (the launcher shortens the run when a launch would otherwise leave
+// SMs idle: the last panels of the large fronts near the root),
 // warp-specialized:
 //   warps 0-7 (two per TMEM lane quarter, each with half of the columns)
 //     first write the tile's A' rows (hi and lo TF32 parts of the L panel,
@@ -182,7 +184,8 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 // Every wait is bounded; on time-out a thread records an error, the
 // producer waits (bounded) for the copies it issued, and the CTA frees its
 // tensor memory and returns.
-constexpr int kColTilesPerCta = 16;
+constexpr int kColTilesPerCta = 16;  // longest column run of a CTA
+constexpr int kMinColTiles = 2;      // shortest (the A' rows are loaded once per run)
 constexpr int kStages = 3;
 constexpr uint32_t kStageBytes = 2 * kBTileBytes;
 constexpr uint32_t kSmemBytes = kStages * kStageBytes + 256;
@@ -202,7 +205,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // the same SM beside it; shared memory fits likewise (196.9 + 33.3 KB).
 __global__ void __maxnreg__(128)
     k_schur_tc(const TcFront *__restrict__ fr, c64 *pool, int f_begin, int k0, int ct_lo, int ct_hi,
-               const uint8_t *scratch, int *err) {
+               const uint8_t *scratch, int *err, int cpc) {
     extern __shared__ __align__(1024) uint8_t smem[];
     const TcFront f = fr[f_begin + blockIdx.x];
     const int w = min(kPanel, f.p - k0);
@@ -210,9 +213,9 @@ __global__ void __maxnreg__(128)
     const int t0 = k0 + w, mt = f.m - t0;
     const int rt = blockIdx.y;
     const int cts = min((mt + kTileNc - 1) / kTileNc, ct_hi);
-    const int ct0 = ct_lo + blockIdx.z * kColTilesPerCta;
+    const int ct0 = ct_lo + blockIdx.z * cpc;
     if (rt * kTileM >= mt || ct0 >= cts) return;
-    const int J = min(kColTilesPerCta, cts - ct0);
+    const int J = min(cpc, cts - ct0);
 
     uint8_t *b_base = smem;
     uint64_t *bars = (uint64_t *)(smem + kStages * kStageBytes);
@@ -400,9 +403,20 @@ int tc_schur_cols(const TcFront *fr, c64 *pool, int f_begin, int nfl, int k0, in
     const int rts = (max_trail + kTileM - 1) / kTileM;
     const int cts = std::min((max_trail + kTileNc - 1) / kTileNc, ct_hi) - ct_lo;
     if (rts < 1 || cts < 1) return FDFD_OK;
-    const int cgs = (cts + tc::kColTilesPerCta - 1) / tc::kColTilesPerCta;
+    // column run per CTA: the longest that still gives about two CTAs per SM
+    // (one CTA is resident per SM: TMEM and shared memory), at least two tiles
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        sms = (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0) ? n : 152;
+    }
+    const int64_t tiles = (int64_t)nfl * rts * cts;
+    const int cpc = (int)std::max<int64_t>(tc::kMinColTiles,
+                                           std::min<int64_t>(tc::kColTilesPerCta, (tiles + 2 * sms - 1) / (2 * sms)));
+    const int cgs = (cts + cpc - 1) / cpc;
     tc::k_schur_tc<<<dim3(nfl, rts, cgs), tc::kCtaThreads, tc::kSmemBytes, st>>>(fr, pool, f_begin, k0, ct_lo,
-                                                                                ct_hi, scratch, err);
+                                                                                ct_hi, scratch, err, cpc);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(FDFD_ERR_CUDA, std::string("schur_tc: ") + cudaGetErrorString(e));
     return FDFD_OK;

@@ -294,22 +294,30 @@ class Simulation:
 
     # ---- design regions (simulation.py:344-369) ---------------------------------
     def init_design_region(self, design_region, eps_m, style=''):
-        if style == 'full':
-            eps_full = eps_m * np.ones(self.eps_r.shape)
-            eps_full[design_region == 0] = self.eps_r[design_region == 0]
-            self.eps_r = eps_full
-        elif style == 'halfway':
-            eps_halfway = self.eps_r
-            eps_halfway[design_region == 1] = eps_m / 2 + 1 / 2
-            self.eps_r = eps_halfway
-        elif style == 'empty':
-            eps_empty = np.ones(self.eps_r.shape)
-            eps_empty[design_region == 0] = self.eps_r[design_region == 0]
-            self.eps_r = eps_empty
-        elif style == 'random':
-            eps_random = (eps_m - 1) * np.random.random(self.eps_r.shape) + 1
-            eps_random[design_region == 0] = self.eps_r[design_region == 0]
-            self.eps_r = eps_random
+        """Initial permittivity of a design region (simulation.py:344-369):
+        inside the region (design_region != 0) eps_r becomes eps_m ('full'),
+        1 ('empty'), uniform random in [1, eps_m) from numpy's global RNG
+        ('random'), or (eps_m + 1) / 2 where design_region == 1, written into
+        the current eps_r array itself ('halfway'); outside it stays.  Any
+        other style leaves eps_r unchanged.  Setting eps_r rebuilds the
+        device operator, as the reference's setter rebuilds A."""
+        region = np.asarray(design_region)
+        if style == 'halfway':
+            new = self.eps_r                     # the reference modifies the array in place
+            new[region == 1] = eps_m / 2 + 1 / 2
+        elif style in ('full', 'empty', 'random'):
+            shape = self.eps_r.shape
+            if style == 'full':
+                new = eps_m * np.ones(shape)
+            elif style == 'empty':
+                new = np.ones(shape)
+            else:
+                new = (eps_m - 1) * np.random.random(shape) + 1
+            outside = region == 0
+            new[outside] = self.eps_r[outside]
+        else:
+            return
+        self.eps_r = new
 
     def __deepcopy__(self, memo):
         # device handles are not deep-copyable; copy host state and rebuild

@@ -21,7 +21,8 @@ Kerr fixture; `--only hz2048` writes the sampled fixture of the 2048 x 2048
 Hz solve (about 15 minutes and 40 GB of host memory: the reference's
 default solver path through the exact-LU shim, then FP64 iterative
 refinement with the same factor); `--only kerr_sweep` the Kerr Newton
-amplitude sweep at 128 x 128 (a few minutes).
+amplitude sweep at 128 x 128 (a few minutes); `--only design` the outputs
+of init_design_region.
 """
 from __future__ import annotations
 
@@ -287,6 +288,26 @@ def kerr_sweep_golden(N=128, n_sample=2048):
     np.savez_compressed(OUT / f"kerr{N}_sweep.npz", **out)
 
 
+def design_golden():
+    """Simulation.init_design_region of the reference (simulation.py:344-369)
+    for each style on a small grid with a random eps_r and design region;
+    numpy's global RNG is seeded with 5 before each call ('random' draws
+    from it)."""
+    from fdfdpy import Simulation
+    from fdfdpy.constants import C_0
+    rng = np.random.default_rng(9)
+    eps = 1 + 3 * rng.random((20, 16))
+    region = np.zeros((20, 16))
+    region[5:14, 4:11] = 1
+    out = {"eps": eps, "region": region}
+    for style in ("full", "halfway", "empty", "random", "other"):
+        sim = Simulation(2 * np.pi * C_0 / 1.55e-6, eps.copy(), 0.02, [3, 3], "Ez")
+        np.random.seed(5)
+        sim.init_design_region(region, 7.5, style=style)
+        out[style] = np.array(sim.eps_r)
+    np.savez_compressed(OUT / "design.npz", **out)
+
+
 def projection_vectors(n, count, seed=2048):
     """`count` complex Gaussian vectors of length n with E|g.v|^2 = ||v||^2,
     generated one after the other from numpy's PCG64 stream (identical on
@@ -357,7 +378,7 @@ if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None, help="path of the reference checkout")
-    ap.add_argument("--only", default=None, choices=["kerr", "hz2048", "kerr_sweep"])
+    ap.add_argument("--only", default=None, choices=["kerr", "hz2048", "kerr_sweep", "design"])
     a = ap.parse_args()
     if a.reference:
         REF = a.reference
@@ -365,7 +386,8 @@ if __name__ == "__main__":
         install_shims()
         import warnings
         warnings.simplefilter("ignore")
-        {"kerr": kerr_golden, "hz2048": hz2048_golden, "kerr_sweep": kerr_sweep_golden}[a.only]()
+        {"kerr": kerr_golden, "hz2048": hz2048_golden, "kerr_sweep": kerr_sweep_golden,
+         "design": design_golden}[a.only]()
         print("golden vectors written to", OUT)
     else:
         main()

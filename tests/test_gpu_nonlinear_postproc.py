@@ -201,3 +201,19 @@ def test_design_region_optimisation_step_increases_objective():
         Js.append(Jk)
     assert Js[-1] > Js[0], Js
     assert sim.eps_r[region == 0].max() == 1.0 and 1.0 <= sim.eps_r.min() and sim.eps_r.max() <= 6.0
+
+
+def test_init_design_region_matches_reference():
+    """init_design_region for every style against the reference's own
+    outputs (tests/golden/design.npz; numpy's RNG seeded alike)."""
+    from pathlib import Path
+    from fdfdpy_gb300 import Simulation
+    g = np.load(Path(__file__).resolve().parent / "golden" / "design.npz")
+    for style in ("full", "halfway", "empty", "random", "other"):
+        eps = g["eps"].copy()
+        sim = Simulation(OMEGA, eps, 0.02, [3, 3], "Ez")
+        np.random.seed(5)
+        sim.init_design_region(g["region"], 7.5, style=style)
+        assert np.array_equal(sim.eps_r, g[style]), style
+        if style == "halfway":
+            assert sim.eps_r is eps                 # modified in place, as the reference does
