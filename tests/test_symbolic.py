@@ -150,3 +150,49 @@ def test_flop_and_size_counts_2048():
     # complex LU flops of the whole tree: order n^1.5 (nested dissection)
     assert 1e11 < info.factor_flops < 1e13
     assert info.pool_entries < 3e9
+
+
+@pytest.mark.parametrize("Nx,Ny,leaf,B", [(8, 8, 4, 2), (17, 23, 16, 3), (40, 33, 64, 4)])
+def test_batch_forest_replicates_the_tree(Nx, Ny, leaf, B):
+    """The batch symbolic (one forest of B copies of the tree, for factoring B
+    operators of a grid in one pass) is the single tree B times: level L
+    holds the B copies of the tree's level-L fronts contiguously, copy b's
+    variables are the tree's plus b n, its children / parents stay inside
+    the copy, and the neighbour and extend-add maps are the tree's."""
+    one = engine.Symbolic(Nx, Ny, leaf)
+    fst = engine.Symbolic(Nx, Ny, leaf, batch=B)
+    n = Nx * Ny
+    assert fst.info.Nx == B * Nx and fst.info.Ny == Ny
+    assert fst.info.n_fronts == B * one.info.n_fronts and fst.info.n_levels == one.info.n_levels
+    assert fst.info.factor_flops == pytest.approx(B * one.info.factor_flops)
+    nf1, nf = one.info.n_fronts, fst.info.n_fronts
+    a = dict(p=one.export(0, nf1), m=one.export(1, nf1), parent=one.export(2, nf1), c0=one.export(3, nf1),
+             voff=one.export(6, nf1), lp=one.export(7, one.info.n_levels + 1), vars=one.export(8, one.info.sum_m),
+             relmap=one.export(9, one.info.sum_m), nbr=one.export(10, 4 * n), vfront=one.export(11, n),
+             vloc=one.export(12, n))
+    b = dict(p=fst.export(0, nf), m=fst.export(1, nf), parent=fst.export(2, nf), c0=fst.export(3, nf),
+             voff=fst.export(6, nf), lp=fst.export(7, fst.info.n_levels + 1), vars=fst.export(8, fst.info.sum_m),
+             relmap=fst.export(9, fst.info.sum_m), nbr=fst.export(10, 4 * n * B), vfront=fst.export(11, n * B),
+             vloc=fst.export(12, n * B))
+    assert np.array_equal(b["lp"], B * a["lp"])
+    for L in range(one.info.n_levels):
+        cnt = a["lp"][L + 1] - a["lp"][L]
+        for copy in range(B):
+            for f in range(a["lp"][L], a["lp"][L + 1]):
+                g = b["lp"][L] + copy * cnt + (f - a["lp"][L])
+                assert b["p"][g] == a["p"][f] and b["m"][g] == a["m"][f]
+                va = a["vars"][a["voff"][f]:a["voff"][f] + a["m"][f]]
+                vb = b["vars"][b["voff"][g]:b["voff"][g] + b["m"][g]]
+                assert np.array_equal(vb, va + copy * n)
+                assert np.array_equal(b["relmap"][b["voff"][g]:b["voff"][g] + b["m"][g]],
+                                      a["relmap"][a["voff"][f]:a["voff"][f] + a["m"][f]])
+                if a["parent"][f] >= 0:
+                    pg = b["parent"][g]
+                    assert b["lp"][L + 1] <= pg and vb[0] // n == copy
+                    assert b["vars"][b["voff"][pg]] // n == copy     # the parent is in the same copy
+    assert np.array_equal(b["nbr"], np.tile(a["nbr"], B))
+    assert np.array_equal(b["vloc"], np.tile(a["vloc"], B))
+    for copy in range(B):
+        cells = np.arange(n) + copy * n
+        owner = b["vfront"][cells]
+        assert np.all(b["vars"][b["voff"][owner] + b["vloc"][cells]] == cells)
