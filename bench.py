@@ -329,7 +329,7 @@ def run_reference(args):
     power-law extrapolation, labelled as such."""
     N = args.size
     ts, a, t_pred = cpu_sample((args.cpu_sample // 2, args.cpu_sample), N)
-    cap = float(os.environ.get("FDFD_REF_MAX_S", "1650"))
+    cap = float(os.environ.get("FDFD_REF_MAX_S", "1700"))
     full = None
     try:
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--reference-full-solve", str(N)],

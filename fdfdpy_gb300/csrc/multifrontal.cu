@@ -1642,6 +1642,7 @@ struct fdfd_factor {
     // is the factor's own), with the settings it was captured under
     bool use_graphs = true;
     cudaGraphExec_t graph = nullptr;
+    cudaStream_t st_cap = nullptr;  // the stream the sequence is captured on
     double graph_pivot_tol = 0.0;
     int graph_fused = 0;
     long long graph_launches[PROF_NCLASS] = {};
@@ -1819,12 +1820,22 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
 // index lists, coefficient store, scratch, the look-ahead stream's events),
 // so the graph captured at the first call is replayed by every later one;
 // only the coefficient evaluation (k_coef, which reads the caller's
-// operator buffers) runs outside it.  A graph is not used while per-class
-// profiling is on (replays are not timed per class), for an explicit-
-// stencil operator read in place, or once a capture has failed.
+// operator buffers) runs outside it.  The capture runs on a stream of the
+// factor's own (capturing records launches without running them, and the
+// caller's stream may be the legacy default stream, which cannot be
+// captured); the graph is then launched on the caller's stream.  A graph is
+// not used while per-class profiling is on (replays are not timed per
+// class), for an explicit-stencil operator read in place, while the
+// caller's stream is itself being captured (its graph takes the launches),
+// or once a capture has failed.
 template <typename T, typename R>
 int factor_levels_graphed(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     if (!fac->use_graphs || prof_enabled() || o.stencil != fac->d_coef) return factor_levels<T, R>(fac, o, st);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return factor_levels<T, R>(fac, o, st);
+    }
     if (fac->graph && fac->graph_pivot_tol == fac->pivot_tol && fac->graph_fused == fac->fused_max_m) {
         CUDA_TRY(cudaGraphLaunch(fac->graph, st));
         for (int c = 0; c < PROF_NCLASS; ++c) prof_count(c, fac->graph_launches[c]);
@@ -1843,15 +1854,22 @@ int factor_levels_graphed(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     og.stencil = fac->d_coef;
     long long before[PROF_NCLASS];
     for (int c = 0; c < PROF_NCLASS; ++c) before[c] = prof_launches(c);
-    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    const int rc = factor_levels<T, R>(fac, og, st);
+    if ((!fac->st_cap && cudaStreamCreateWithFlags(&fac->st_cap, cudaStreamNonBlocking) != cudaSuccess) ||
+        cudaStreamBeginCapture(fac->st_cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        fac->use_graphs = false;
+        return factor_levels<T, R>(fac, o, st);
+    }
+    const int rc = factor_levels<T, R>(fac, og, fac->st_cap);
     cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(st, &g);
+    cudaError_t e = cudaStreamEndCapture(fac->st_cap, &g);
     if (rc == FDFD_OK && e == cudaSuccess) e = cudaGraphInstantiate(&fac->graph, g, 0);
     if (g) cudaGraphDestroy(g);
     if (rc != FDFD_OK || e != cudaSuccess) {
-        // not capturable here: launch directly from now on
+        // not capturable here: launch directly from now on (the launch
+        // counts of the failed capture are taken back)
         cudaGetLastError();
+        for (int c = 0; c < PROF_NCLASS; ++c) prof_count(c, before[c] - prof_launches(c));
         fac->graph = nullptr;
         fac->use_graphs = false;
         return factor_levels<T, R>(fac, o, st);
@@ -2481,6 +2499,7 @@ int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, in
 
 void free_factor(fdfd_factor *f) {
     if (f && f->graph) cudaGraphExecDestroy(f->graph);
+    if (f && f->st_cap) cudaStreamDestroy(f->st_cap);
     if (!f) return;
     void *ptrs[] = {f->d_inv, f->d_piv, f->d_fronts, f->d_vars, f->d_relmap, f->d_nbr, f->d_vfront, f->d_vloc, f->d_pool,
                     f->d_W, f->d_Y, f->d_r, f->d_d, f->d_tmp, f->d_isxf, f->d_isyf, f->d_partial,

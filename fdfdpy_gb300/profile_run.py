@@ -91,9 +91,15 @@ def stencil_passes(op, N, om):
     kerr = KerrTerms(om, 1e-6, op.eps, [Nonlinearity(2.8e-6, region)])
     flux = torch.empty((), dtype=torch.float64, device="cuda")
 
+    # the refinement's residual form: explicit (stored) coefficients
+    coef = (torch.randn(5, N * N, generator=g, dtype=torch.float64)
+            + 1j * torch.randn(5, N * N, generator=g, dtype=torch.float64)).cuda()
+    op_st = engine.StencilOperator(N, N, coef)
+
     def run():
         op.csr_device()
         op.residual(x, x)
+        op_st.apply(x)
         op.fields(x)
         op.grad_eps(x, x)
         kerr(x, eps_nl=True, jac=True)
