@@ -10,9 +10,12 @@ launch configuration of the serving path:
   takes; larger fronts go through the per-panel TRSM / Schur tiles).
 
 Each candidate factors B synthetic operators of the grid (eps_r in 8 x 8
-blocks of {1, 12.25}, the serving workload's family) and refines `nrhs`
-right-hand sides per problem; the score is right-hand sides solved per
-second of device time (CUDA events).  Results are cached per (shape,
+blocks of {1, 12.25}, the serving workload's family) and refines their
+right-hand sides: `nrhs` per problem, or -- for `nrhs = (lo, hi)`, the
+serving stream's spread -- a seeded draw in [lo, hi] per problem, so that
+a batch pays for padding its members to the largest count as it does in
+service; the score is right-hand sides solved per second of device time
+(CUDA events).  Results are cached per (shape,
 precision) in memory and, when `path` is given, in a JSON file that later
 processes read instead of timing again.
 """
@@ -31,10 +34,11 @@ from .constants import C_0
 
 class Autotuner:
 
-    def __init__(self, batches=(1, 2, 4, 8), fused_limits=(-1, 128), nrhs=4, path=None, memory_fraction=0.25,
+    def __init__(self, batches=(1, 2, 4, 8), fused_limits=(-1, 128), nrhs=(1, 8), path=None, memory_fraction=0.25,
                  pol="Hz", npml=(10, 10), dl=0.02):
         self.batches, self.fused_limits = tuple(batches), tuple(fused_limits)
-        self.nrhs, self.path, self.memory_fraction = int(nrhs), path, float(memory_fraction)
+        self.nrhs = (int(nrhs), int(nrhs)) if np.isscalar(nrhs) else (int(nrhs[0]), int(nrhs[1]))
+        self.path, self.memory_fraction = path, float(memory_fraction)
         self.pol, self.npml, self.dl = pol, tuple(npml), float(dl)
         self.table: dict = {}
         self._lock = threading.Lock()
@@ -66,7 +70,8 @@ class Autotuner:
         for _ in range(B):
             eps = np.kron(rng.choice([1.0, 12.25], size=(-(-Nx // 8), -(-Ny // 8))), np.ones((8, 8)))[:Nx, :Ny]
             ops.append(engine.DeviceOperator(om, eps, Nx * self.dl, Ny * self.dl, self.npml, self.pol, 1e-6))
-        rhs = [torch.randn(self.nrhs, Nx * Ny, dtype=torch.complex128, device=engine.device()) for _ in range(B)]
+        counts = rng.integers(self.nrhs[0], self.nrhs[1] + 1, size=B)
+        rhs = [torch.randn(int(k), Nx * Ny, dtype=torch.complex128, device=engine.device()) for k in counts]
         return ops, rhs
 
     def _time(self, shape, precision, B, fused, reps=2):
@@ -95,7 +100,7 @@ class Autotuner:
             torch.cuda.synchronize()
             best = min(best, e0.elapsed_time(e1))
         del fac
-        return best
+        return best, sum(int(r.shape[0]) for r in rhs)
 
     def tune(self, shape, precision):
         """Time every candidate that fits in memory; record and return the
@@ -107,9 +112,8 @@ class Autotuner:
             if need > self.memory_fraction * free:
                 continue
             for fused in self.fused_limits:
-                ms = self._time(shape, precision, B, fused)
-                results.append({"batch": B, "fused_max_m": fused, "ms": ms,
-                                "solves_per_s": 1e3 * B * self.nrhs / ms})
+                ms, solves = self._time(shape, precision, B, fused)
+                results.append({"batch": B, "fused_max_m": fused, "ms": ms, "solves_per_s": 1e3 * solves / ms})
         engine.release_cached_factors()
         if not results:
             results = [{"batch": 1, "fused_max_m": -1, "ms": float("nan"), "solves_per_s": float("nan")}]

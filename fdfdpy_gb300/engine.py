@@ -330,6 +330,7 @@ class Factor:
     def numeric(self, op: DeviceOperator):
         s = op.struct()
         N.call("fdfd_factor_numeric", self.handle, C.byref(s), stream_ptr())
+        self._last = None
         self._used()
         self.op = op
         self._op_struct = s
@@ -377,7 +378,7 @@ class Factor:
                                                   int(max_iter), stream_ptr())
             if code != N.FDFD_ERR_NOT_CONVERGED or raise_on_fail:
                 N.check(code, "fdfd_solve_refined")
-            st = self.stats()
+            st = self._raw_stats()
             worst, iters = max(worst, st["rel_residual"]), max(iters, st["refine_iters"])
             outs.append(x)
         self._used()
@@ -388,15 +389,20 @@ class Factor:
         """Counters of the last factorization and solve (the residual and
         refinement count are the worst over the column blocks of the last
         solve call)."""
-        st = N.FactorStats()
-        N.call("fdfd_factor_stats_get", self.handle, C.byref(st))
-        out = {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
-               "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
-               "tc_errors": st.tc_errors}
+        out = self._raw_stats()
         last = getattr(self, "_last", None)
         if last is not None:
-            out["rel_residual"], out["refine_iters"] = max(out["rel_residual"], last[0]), max(out["refine_iters"], last[1])
+            out["rel_residual"], out["refine_iters"] = last
         return out
+
+    def _raw_stats(self) -> dict:
+        """The library's counters of the last factorization and of the last
+        solve call into it (one column block)."""
+        st = N.FactorStats()
+        N.call("fdfd_factor_stats_get", self.handle, C.byref(st))
+        return {"tiny_pivots": st.tiny_pivots, "refine_iters": st.refine_iters,
+                "rel_residual": st.rel_residual, "factor_ms": st.factor_ms, "solve_ms": st.solve_ms,
+                "tc_errors": st.tc_errors}
 
     def __del__(self):
         try:
