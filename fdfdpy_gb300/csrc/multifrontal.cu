@@ -758,31 +758,36 @@ __global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ f
 // blockIdx.y) and, on tensor-core levels (tcf != NULL), its packed tiles.
 // HALF: 32-row (L) / 32-column (U) tiles, twice the CTAs, for levels with
 // few fronts whose triangular updates would not fill the GPU.
-template <typename T, typename R, bool HALF>
+// Q = 4, 2 or 1: output tiles of 16 Q rows (L21) / 16 Q columns (U12).
+template <typename T, typename R, int Q>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
                                                     const TcFront *__restrict__ tcf, uint8_t *scratch) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
     if (blockIdx.z == 0) {
-        gemm_tile<T, R, TRSM_L, HALF ? 2 : 4, 4>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
+        gemm_tile<T, R, TRSM_L, Q, 4>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
     } else {
         uint8_t *bpack = tcf ? scratch + tcf[f_begin + blockIdx.x].b_off : nullptr;
-        gemm_tile<T, R, TRSM_U, 4, HALF ? 2 : 4>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
+        gemm_tile<T, R, TRSM_U, 4, Q>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
     }
 }
 
 // Both triangular updates of panel k0 for the fronts of a level (trail: an
 // upper bound of m - t0).  Half-height tiles while the level would launch
-// fewer than 1024 CTAs.
+// fewer than 1024 CTAs, quarter-height ones below 256 (the last panels of the
+// few large fronts near the root, on the factorization's critical path).
 template <typename T, typename R>
 void trsm_launch(int nfl, int trail, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0,
                  const TcFront *tcf, uint8_t *scratch) {
     const int tiles = (trail + BM - 1) / BM;
-    if (nfl * tiles * 2 < 1024) {
+    if (nfl * tiles * 2 < 256) {
+        const int t4 = (trail + BM / 4 - 1) / (BM / 4);
+        k_trsm_panel<T, R, 1><<<dim3(nfl, t4, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+    } else if (nfl * tiles * 2 < 1024) {
         const int t2 = (trail + BM / 2 - 1) / (BM / 2);
-        k_trsm_panel<T, R, true><<<dim3(nfl, t2, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+        k_trsm_panel<T, R, 2><<<dim3(nfl, t2, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     } else {
-        k_trsm_panel<T, R, false><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+        k_trsm_panel<T, R, 4><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     }
 }
 
