@@ -556,260 +556,6 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
         for (int r = lane; r < n; r += 32) G[r + (int64_t)c * ld] = D[r + c * LD];
 }
 
-// ---- the 64 x 64 diagonal block of a panel step, blocked by 16 ------------
-// The same result as k_dense_lu with whole = 0 (LU without row exchanges, a
-// pivot below `tiny` lifted and counted, then inv(L) strictly below and
-// inv(U) on and above the diagonal, in place) with far fewer block-wide
-// barriers: four steps of a 16-wide right-looking blocked LU, each
-//   1. warp 0 factors the 16 x 16 diagonal block (rank-1 steps separated by
-//      __syncwarp only) and replaces it by its two triangular inverses
-//      (lanes 0-15 a column of inv(L) each, lanes 16-31 a row of inv(U)),
-//   2. all threads form L below (A inv(U_kk)) and U right of it
-//      (inv(L_kk) A), operands read into registers before any write,
-//   3. all threads apply the rank-16 update to the trailing block,
-// then the off-diagonal blocks of the inverses are completed block row by
-// block row: X_ij = -inv(L_ii) sum_{k=j}^{i-1} L_ik X_kj and
-// Y_ji = -(sum_{k=j}^{i-1} Y_jk U_ki) inv(U_ii).  About 22 barriers instead
-// of about 78 for the 4-pivot steps; the block sits on the critical path of
-// the last panel steps of the large fronts near the root.
-constexpr int kDB = 16;        // block size
-constexpr int kDLD = NB + 1;   // leading dimension in shared memory
-
-template <typename T, typename R>
-__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1)
-    k_diag_lu(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0, R tiny, int *tiny_count) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *D = reinterpret_cast<T *>(smem_raw);
-    const FrontD f = fr[f_begin + blockIdx.x];
-    const int P = min(NB, f.p - k0);
-    if (P <= 0) return;
-    const int64_t ld = f.ld;
-    T *G = pool + f.f_off + (int64_t)k0 * ld + k0;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int c = warp; c < NB; c += 8)
-        for (int r = lane; r < NB; r += 32)
-            D[r + c * kDLD] = (r < P && c < P) ? G[r + (int64_t)c * ld] : (r == c ? cone<T>() : czero<T>());
-    __syncthreads();
-    const int nb = (P + kDB - 1) / kDB;  // blocks holding pivots (the rest is identity)
-    const R tiny2 = tiny * tiny;
-    for (int kb = 0; kb < nb; ++kb) {
-        const int b0 = kb * kDB;
-        T *Dk = D + b0 + b0 * kDLD;  // the diagonal block
-        if (warp == 0) {
-            const int i = lane & 15, h = lane >> 4;
-            for (int j = 0; j < kDB; ++j) {
-                T piv = Dk[j + j * kDLD];
-                const bool lift = !(cabs2(piv) >= tiny2);
-                if (lift) {
-                    const R am = sqrt(cabs2(piv));
-                    piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
-                }
-                const T pinv = crecip_fast(piv);
-                // rows i > j: multiplier and the rank-1 update of their entries
-                // right of column j (the two lanes of a row split the columns)
-                T l = czero<T>();
-                if (i > j) {
-                    l = cmul(Dk[i + j * kDLD], pinv);
-                    for (int k = j + 1 + h; k < kDB; k += 2) cmsub(Dk[i + k * kDLD], l, Dk[j + k * kDLD]);
-                }
-                __syncwarp(0xffffffffu);  // every read of column j and of the pivot is done
-                if (i > j && h == 0) Dk[i + j * kDLD] = l;
-                if (lift && lane == 0) {
-                    Dk[j + j * kDLD] = piv;
-                    atomicAdd(tiny_count, 1);
-                }
-                __syncwarp(0xffffffffu);
-            }
-            // lanes 0-15: column q of inv(L) (unit lower); lanes 16-31: row q of inv(U)
-            const int q = lane & 15;
-            T v[kDB];
-            if (h == 0) {
-#pragma unroll
-                for (int r = 0; r < kDB; ++r) v[r] = (r == q) ? cone<T>() : czero<T>();
-#pragma unroll
-                for (int t = 0; t < kDB; ++t)
-#pragma unroll
-                    for (int r = 0; r < kDB; ++r)
-                        if (t >= q && r > t) cmsub(v[r], Dk[r + t * kDLD], v[t]);
-            } else {
-#pragma unroll
-                for (int c = 0; c < kDB; ++c) {
-                    T acc = (c == q) ? cone<T>() : czero<T>();
-#pragma unroll
-                    for (int k = 0; k < kDB; ++k)
-                        if (k >= q && k < c) cmsub(acc, v[k], Dk[k + c * kDLD]);
-                    v[c] = (c >= q) ? cmul(acc, crecip_fast(Dk[c + c * kDLD])) : czero<T>();
-                }
-            }
-            __syncwarp(0xffffffffu);
-            if (h == 0) {
-#pragma unroll
-                for (int r = 0; r < kDB; ++r)
-                    if (r > q) Dk[r + q * kDLD] = v[r];
-            } else {
-#pragma unroll
-                for (int c = 0; c < kDB; ++c)
-                    if (c >= q) Dk[q + c * kDLD] = v[c];
-            }
-        }
-        __syncthreads();
-        // L below (rows b0+16..NB-1, 4 columns an item) and U right (columns
-        // b0+16..NB-1, 4 rows an item); at most 384 items: two per thread
-        const int t0 = b0 + kDB, nr = NB - t0;
-        if (nr > 0) {
-            T out[2][4];
-            int item[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int it = tid + 256 * u;
-                item[u] = it < 8 * nr ? it : -1;
-                if (item[u] < 0) continue;
-                const int lower = it < 4 * nr, e = lower ? it : it - 4 * nr;
-                const int line = t0 + e / 4, g = 4 * (e % 4);
-                T a[kDB];
-#pragma unroll
-                for (int t = 0; t < kDB; ++t) a[t] = lower ? D[line + (b0 + t) * kDLD] : D[(b0 + t) + line * kDLD];
-#pragma unroll
-                for (int o = 0; o < 4; ++o) {
-                    const int c = g + o;
-                    T acc = czero<T>();
-                    if (lower) {  // (A inv(U_kk))[line, c]: inv(U) is upper (t <= c)
-#pragma unroll
-                        for (int t = 0; t < kDB; ++t)
-                            if (t <= c) cmac(acc, a[t], Dk[t + c * kDLD]);
-                    } else {      // (inv(L_kk) A)[c, line]: inv(L) unit lower (t <= c)
-#pragma unroll
-                        for (int t = 0; t < kDB; ++t) {
-                            if (t < c) cmac(acc, Dk[c + t * kDLD], a[t]);
-                            else if (t == c) acc = cadd(acc, a[t]);
-                        }
-                    }
-                    out[u][o] = acc;
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                if (item[u] < 0) continue;
-                const int it = item[u];
-                const int lower = it < 4 * nr, e = lower ? it : it - 4 * nr;
-                const int line = t0 + e / 4, g = 4 * (e % 4);
-#pragma unroll
-                for (int o = 0; o < 4; ++o) {
-                    if (lower) D[line + (b0 + g + o) * kDLD] = out[u][o];
-                    else D[(b0 + g + o) + line * kDLD] = out[u][o];
-                }
-            }
-            __syncthreads();
-            // trailing block [t0, NB)^2 -= L[:, b0:b0+16] U[b0:b0+16, :]
-            const int tx = tid & 15, ty = tid >> 4, nq = nr / kDB;
-            T acc[3][3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int b = 0; b < 3; ++b) acc[a][b] = czero<T>();
-#pragma unroll
-            for (int t4 = 0; t4 < kDB; t4 += 4) {
-                T l[3][4], uu[4][3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int t = 0; t < 4; ++t)
-                        l[a][t] = a < nq ? D[(t0 + ty + kDB * a) + (b0 + t4 + t) * kDLD] : czero<T>();
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-#pragma unroll
-                    for (int b = 0; b < 3; ++b)
-                        uu[t][b] = b < nq ? D[(b0 + t4 + t) + (t0 + tx + kDB * b) * kDLD] : czero<T>();
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int b = 0; b < 3; ++b)
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) cmac(acc[a][b], l[a][t], uu[t][b]);
-            }
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int b = 0; b < 3; ++b)
-                    if (a < nq && b < nq) {
-                        T &e = D[(t0 + ty + kDB * a) + (t0 + tx + kDB * b) * kDLD];
-                        e = csub(e, acc[a][b]);
-                    }
-            __syncthreads();
-        }
-    }
-    // off-diagonal blocks of the inverses, block row (column) ib at a time
-    const int tx = tid & 15, ty = tid >> 4;
-    for (int ib = 1; ib < nb; ++ib) {
-        const int bi = ib * kDB;
-        // S_j = sum_{k=j}^{ib-1} L[ib, k] X[k, j] (lower), T_j = sum_k Y[j, k] U[k, ib] (upper)
-        T sl[3], su[3];
-#pragma unroll
-        for (int jb = 0; jb < 3; ++jb) {
-            if (jb >= ib) break;
-            const int bj = jb * kDB;
-            T a = czero<T>(), b = czero<T>();
-            for (int kb2 = jb; kb2 < ib; ++kb2) {
-                const int bk = kb2 * kDB;
-#pragma unroll 4
-                for (int t = 0; t < kDB; ++t) {
-                    // X[bk + t, bj + tx]: unit lower inverse inside the diagonal block
-                    T x;
-                    if (kb2 == jb) x = (t > tx) ? D[(bk + t) + (bj + tx) * kDLD] : (t == tx ? cone<T>() : czero<T>());
-                    else x = D[(bk + t) + (bj + tx) * kDLD];
-                    cmac(a, D[(bi + ty) + (bk + t) * kDLD], x);
-                    // Y[bj + ty, bk + t]: upper inverse inside the diagonal block
-                    T y;
-                    if (kb2 == jb) y = (t >= ty) ? D[(bj + ty) + (bk + t) * kDLD] : czero<T>();
-                    else y = D[(bj + ty) + (bk + t) * kDLD];
-                    cmac(b, y, D[(bk + t) + (bi + tx) * kDLD]);
-                }
-            }
-            sl[jb] = a;
-            su[jb] = b;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int jb = 0; jb < 3; ++jb) {
-            if (jb >= ib) break;
-            const int bj = jb * kDB;
-            D[(bi + ty) + (bj + tx) * kDLD] = sl[jb];
-            D[(bj + ty) + (bi + tx) * kDLD] = su[jb];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int jb = 0; jb < 3; ++jb) {
-            if (jb >= ib) break;
-            const int bj = jb * kDB;
-            // X[ib, jb][ty, tx] = -(S + sum_{t < ty} invL_ii[ty, t] S[t, tx])
-            T a = D[(bi + ty) + (bj + tx) * kDLD];
-            for (int t = 0; t < ty; ++t) cmac(a, D[(bi + ty) + (bi + t) * kDLD], D[(bi + t) + (bj + tx) * kDLD]);
-            sl[jb] = cmake<R>(-a.x, -a.y);
-            // Y[jb, ib][ty, tx] = -sum_{t <= tx} T[ty, t] invU_ii[t, tx]
-            T b = czero<T>();
-            for (int t = 0; t <= tx; ++t) cmac(b, D[(bj + ty) + (bi + t) * kDLD], D[(bi + t) + (bi + tx) * kDLD]);
-            su[jb] = cmake<R>(-b.x, -b.y);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int jb = 0; jb < 3; ++jb) {
-            if (jb >= ib) break;
-            const int bj = jb * kDB;
-            D[(bi + ty) + (bj + tx) * kDLD] = sl[jb];
-            D[(bj + ty) + (bi + tx) * kDLD] = su[jb];
-        }
-        __syncthreads();
-    }
-    for (int c = warp; c < P; c += 8)
-        for (int r = lane; r < P; r += 32) G[r + (int64_t)c * ld] = D[r + c * kDLD];
-}
-
-template <typename T>
-constexpr size_t diag_lu_smem() {
-    return (size_t)NB * kDLD * sizeof(T);
-}
-
 // Launch k_dense_lu for blocks padded to S.  The 64-wide panel blocks and
 // the leaves' 80-row fronts have their own builds (about 10% faster there;
 // larger fixed sizes ran slower than the generic build).
@@ -830,10 +576,6 @@ void dense_lu_launch(int nfl, int S, cudaStream_t st, const FrontD *fr, T *pool,
         else
             k_dense_lu<T, R, 0, true><<<nfl, kDenseThreads, smem, st>>>(
                 fr, pool, fb, k0, whole, blocked, tiny, tiny_count, la.o, la.vars, la.nbr_loc, la.maxdiag);
-        return;
-    }
-    if (!whole && S == NB) {
-        k_diag_lu<T, R><<<nfl, 256, diag_lu_smem<T>(), st>>>(fr, pool, fb, k0, tiny, tiny_count);
         return;
     }
     switch (S) {
@@ -2544,8 +2286,6 @@ template <typename T, typename R>
 int set_smem_attrs() {
     CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
-    CUDA_TRY(cudaFuncSetAttribute(k_diag_lu<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)diag_lu_smem<T>()));
     CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDenseSmemMax));
     CUDA_TRY(cudaFuncSetAttribute(k_dense_lu<T, R, 80, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
