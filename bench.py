@@ -588,7 +588,7 @@ def main():
     ap.add_argument("--precision", default="c64tc", choices=["c64tc", "c64", "c128"])
     ap.add_argument("--method", default="ir", choices=["ir", "gmres"])
     ap.add_argument("--requests", type=int, default=512)
-    ap.add_argument("--serving-requests", type=int, default=128)
+    ap.add_argument("--serving-requests", type=int, default=256)
     ap.add_argument("--rate", type=float, default=50.0)
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--batch-max", type=int, default=8, help="problems per forest factorization (1: none)")

@@ -89,7 +89,14 @@ class Autotuner:
             def step():
                 fac.numeric(ops[0])
                 fac.solve(rhs[0], tol=1e-10, max_iter=40)
-        step()                                    # warm-up (first touch, module load)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        step()                                    # warm-up (first touch, graph capture, module load)
+        t1.record()
+        torch.cuda.synchronize()
+        if t0.elapsed_time(t1) > 250.0:
+            reps = 1                              # long candidates: one timed run is enough
         st = torch.cuda.current_stream()
         best = float("inf")
         for _ in range(reps):
