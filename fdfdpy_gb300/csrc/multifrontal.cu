@@ -1273,9 +1273,9 @@ __device__ __forceinline__ void panel_rows_update(const T *F, int64_t ld, int k0
 // Row-block product for the backward opener: acc[rhs] = sum over columns
 // [c0, c0+cn) of F[row, c] xs[rhs][c - c0] (xs in shared memory, row
 // stride kRowsPerCta), four threads per row as in panel_rows_update.
-template <typename T>
+template <typename T, int N>
 __device__ __forceinline__ void opener_rows_product(const T *F, int64_t ld, int row, bool live, int c0, int cn,
-                                                    const T *xs, int nrhs, T (&acc)[8]) {
+                                                    const T *xs, int nrhs, T (&acc)[N]) {
     const int q = threadIdx.x & 3;
     if (live) {
         for (int cb = 16 * q; cb < cn; cb += 64) {
@@ -1300,8 +1300,8 @@ __device__ __forceinline__ void opener_rows_product(const T *F, int64_t ld, int 
     }
 }
 
-template <typename T>
-__device__ __forceinline__ void quad_reduce(T (&acc)[8], int nrhs) {
+template <typename T, int N>
+__device__ __forceinline__ void quad_reduce(T (&acc)[N], int nrhs) {
     for (int r = 0; r < nrhs; ++r)
         for (int off = 1; off < 4; off <<= 1) {
             acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, off);
@@ -2033,10 +2033,10 @@ __device__ __forceinline__ c128 ldcg_c<c128>(const c128 *p) {
 // panel in order, where v_panel (a 64-vector per rhs) is taken from vsrc
 // (stride sum_m) as its values are published.  The panel's matrix tile is
 // loaded before the wait.
-template <typename T>
+template <typename T, int N>
 __device__ __forceinline__ bool unit_panels(const T *F, int64_t ld, int r0, bool live, int k_first, int k_last,
                                             int k_step, int p, const T *vsrc, int64_t sum_m, int nrhs, int *err,
-                                            unsigned flag_limit, T *vs, T (&acc)[8]) {
+                                            unsigned flag_limit, T *vs, T (&acc)[N]) {
     const int rr = threadIdx.x >> 2, t0 = 16 * (threadIdx.x & 3);
     // the tile of the next panel is loaded while this panel waits and computes
     T a[16], an[16];
@@ -2101,12 +2101,13 @@ __device__ __forceinline__ T diag_rows(const T *Ds, const T *vr, int rn, int row
     return s;
 }
 
-template <typename T, typename R>
+template <typename T, typename R, int NR>
 __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
                 int *err, const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
+    if (NR == 1) nrhs = 1;  // one right-hand side: the sums stay in registers
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
     // gather: right-hand side of the pivots and the children's updates; the
@@ -2162,7 +2163,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         if (piv && live && q == 0)
             for (int r = 0; r < nrhs; ++r) wpre[r * NB + rr] = ldcg_c(W + r * sum_m + f.voff + r0 + rr);
         if (piv) stage_diag<T, false>(F, ld, r0, rn, Ds);
-        T acc[8];
+        T acc[NR];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
         if (!unit_panels(F, ld, r0, live, 0, piv ? rb : KP, 1, f.p, Y + f.voff, sum_m, nrhs, err, flag_limit, vin,
                          acc))
@@ -2186,12 +2187,13 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     }
 }
 
-template <typename T, typename R>
+template <typename T, typename R, int NR>
 __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_bwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxb, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, double2 *x, const int64_t *__restrict__ bwd_off, T *scratch,
                 T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb, int *err,
                 const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
+    if (NR == 1) nrhs = 1;  // one right-hand side: the sums stay in registers
     extern __shared__ unsigned char smem_raw[];
     T *xs = reinterpret_cast<T *>(smem_raw);  // opener: nrhs x kRowsPerCta; panels: panel layout
     const int tid = threadIdx.x;
@@ -2212,7 +2214,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         __syncthreads();
         const int row = rbase + (tid >> 2);
         const bool live = row < f.p;
-        T acc[8];
+        T acc[NR];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
         opener_rows_product(pool + f.f_off, (int64_t)f.ld, row, live, c0, cn, xs, nrhs, acc);
         quad_reduce(acc, nrhs);
@@ -2261,7 +2263,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         if (live && q == 0)
             for (int r = 0; r < nrhs; ++r) wpre[r * NB + rr] = ldcg_c(W + r * sum_m + f.voff + r0 + rr);
         stage_diag<T, true>(F, ld, r0, rn, Ds);
-        T acc[8];
+        T acc[NR];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
         if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, Y + f.voff, sum_m, nrhs, err, flag_limit, vin,
                          acc))
@@ -2298,8 +2300,10 @@ int set_smem_attrs() {
     const int ps = (int)std::max(panel_smem_bytes<T>(8), (size_t)8 * kRowsPerCta * sizeof(T));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_panel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
-    CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
-    CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_fwd_level<T, R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
+    CUDA_TRY(cudaFuncSetAttribute(k_bwd_level<T, R, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
     CUDA_TRY(cudaFuncSetAttribute(k_fwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
     CUDA_TRY(cudaFuncSetAttribute(k_bwd_warp<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmallSmemMax));
@@ -2347,7 +2351,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             // at the co-resident limit
             const int items = std::max(nfl, nunits);
             const int grid = std::max(1, std::min(fac->coop_grid, items));
-            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_fwd_level<T, R>, dim3(grid),
+            CUDA_TRY(cudaLaunchCooperativeKernel(nrhs == 1 ? (const void *)k_fwd_level<T, R, 1> : (const void *)k_fwd_level<T, R, 8>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
@@ -2399,7 +2403,7 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             const int cch = std::max(1, (maxb + kRowsPerCta - 1) / kRowsPerCta);
             const int items = std::max(std::max(nfl * prw * cch, nfl), nunits);
             const int grid = std::max(1, std::min(fac->coop_grid, items));
-            CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_bwd_level<T, R>, dim3(grid),
+            CUDA_TRY(cudaLaunchCooperativeKernel(nrhs == 1 ? (const void *)k_bwd_level<T, R, 1> : (const void *)k_bwd_level<T, R, 8>, dim3(grid),
                                                  dim3(kRowsPerCta), args, sm_coop, st));
             prof_end(PROF_SOLVE_BWD, st, 1);
             continue;
@@ -2676,9 +2680,12 @@ int coop_grid_for(int max_nrhs, int *grid) {
         return FDFD_OK;
     }
     const size_t smem = std::max(panel_smem_bytes<T>(max_nrhs), (size_t)max_nrhs * kRowsPerCta * sizeof(T));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_fwd_level<T, R>, kRowsPerCta, smem));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_bwd_level<T, R>, kRowsPerCta, smem));
-    const int per_sm = std::min(std::min(nb1, nb2), 4);
+    int nb3 = 0, nb4 = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_fwd_level<T, R, 8>, kRowsPerCta, smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb2, k_bwd_level<T, R, 8>, kRowsPerCta, smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb3, k_fwd_level<T, R, 1>, kRowsPerCta, smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb4, k_bwd_level<T, R, 1>, kRowsPerCta, smem));
+    const int per_sm = std::min(std::min(std::min(nb1, nb2), std::min(nb3, nb4)), 4);
     *grid = per_sm > 0 ? per_sm * sms : 0;
     return FDFD_OK;
 }
