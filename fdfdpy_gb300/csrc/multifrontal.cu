@@ -296,36 +296,151 @@ __device__ __forceinline__ void lu4_inv(T *B, int LD, int kw, R tiny, int *tiny_
             for (int j = k + 1; j < kStep; ++j) cmsub(a[i][j], a[i][k], a[k][j]);
         }
     }
-    // inv(L): column q, x = e_q, x[i] -= L[i][t] x[t]
-    T li[kStep][kStep], ui[kStep][kStep];
+    // inverses in place (no second and third 4 x 4 array: a single thread
+    // runs this, and the build's register limit would otherwise spill it).
+    // inv(L), unit lower, column by column from the left: X[i][j] =
+    // -(L[i][j] + sum_{j<k<i} L[i][k] X[k][j]) -- columns right of j still
+    // hold L
 #pragma unroll
-    for (int q = 0; q < kStep; ++q) {
+    for (int j = 0; j < kStep; ++j)
 #pragma unroll
-        for (int i = 0; i < kStep; ++i) li[i][q] = (i == q) ? cone<T>() : czero<T>();
+        for (int i = j + 1; i < kStep; ++i) {
+            T s = a[i][j];
 #pragma unroll
-        for (int t = q; t < kStep; ++t)
-#pragma unroll
-            for (int i = t + 1; i < kStep; ++i) cmsub(li[i][q], a[i][t], li[t][q]);
-    }
-    // inv(U): row r, y[c] = (delta_rc - sum_{r<=k<c} y[k] U[k][c]) / U[c][c]
-#pragma unroll
-    for (int r = 0; r < kStep; ++r)
-#pragma unroll
-        for (int c = 0; c < kStep; ++c) {
-            if (c < r) {
-                ui[r][c] = czero<T>();
-            } else {
-                T s = (c == r) ? cone<T>() : czero<T>();
-#pragma unroll
-                for (int k = r; k < c; ++k) cmsub(s, ui[r][k], a[k][c]);
-                ui[r][c] = cmul(s, dinv[c]);
-            }
+            for (int k = j + 1; k < i; ++k) cmac(s, a[i][k], a[k][j]);
+            a[i][j] = cmake<R>(-s.x, -s.y);
         }
+    // inv(U), row by row from the top: Y[i][i] = 1 / U[i][i], Y[i][j] =
+    // -(sum_{i<=k<j} Y[i][k] U[k][j]) / U[j][j] -- rows below i still hold U,
+    // and U[i][j] is read before it is replaced
+#pragma unroll
+    for (int i = 0; i < kStep; ++i) {
+        a[i][i] = dinv[i];
+#pragma unroll
+        for (int j = i + 1; j < kStep; ++j) {
+            T s = cmul(a[i][i], a[i][j]);
+#pragma unroll
+            for (int k = i + 1; k < j; ++k) cmac(s, a[i][k], a[k][j]);
+            a[i][j] = cmul(cmake<R>(-s.x, -s.y), dinv[j]);
+        }
+    }
 #pragma unroll
     for (int i = 0; i < kStep; ++i)
 #pragma unroll
         for (int j = 0; j < kStep; ++j)
-            if (i < kw && j < kw) B[i + j * LD] = (i > j) ? li[i][j] : ui[i][j];
+            if (i < kw && j < kw) B[i + j * LD] = a[i][j];
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_c(T v, int src) {
+    v.x = __shfl_sync(0xffffffffu, v.x, src);
+    v.y = __shfl_sync(0xffffffffu, v.y, src);
+    return v;
+}
+
+// lu4_inv by one warp: lane i + 4 j (lanes 0-15) holds entry (i, j), so no
+// thread needs the 4 x 4 arrays (the register-tile build keeps its 5 x 5
+// tile live across this).  The same operations in the same order as
+// lu4_inv, entry by entry; the inverses go by distance from the diagonal,
+// reading the factor's entries from o and the inverses' from x.  All 32
+// lanes take part in every shuffle; lanes 16-31 compute nothing used.
+template <typename T, typename R>
+__device__ __forceinline__ void lu4_inv_warp(T *B, int LD, int kw, R tiny, int *tiny_count, int lane) {
+    const int i = lane & 3, j = (lane >> 2) & 3;
+    const bool mine = lane < 16 && i < kw && j < kw;
+    T a = mine ? B[i + j * LD] : (i == j ? cone<T>() : czero<T>());
+    const R tiny2 = tiny * tiny;
+    T dj = cone<T>();  // 1 / U[j][j]
+#pragma unroll
+    for (int k = 0; k < kStep; ++k) {
+        T piv = shfl_c(a, 5 * k);
+        if (!(cabs2(piv) >= tiny2)) {
+            const R am = sqrt(cabs2(piv));
+            piv = (am > R(0)) ? cmake<R>(piv.x / am * tiny, piv.y / am * tiny) : cmake<R>(tiny, R(0));
+            if (lane == 5 * k) {
+                a = piv;
+                atomicAdd(tiny_count, 1);
+            }
+        }
+        const T d = crecip_fast(piv);
+        if (j == k) dj = d;
+        if (j == k && i > k) a = cmul(a, d);
+        const T lik = shfl_c(a, i + 4 * k), akj = shfl_c(a, k + 4 * j);
+        if (i > k && j > k) cmsub(a, lik, akj);
+    }
+    const T o = a;
+    T x = (i == j) ? dj : o;
+    // inv(L), strictly below: X[i][j] = -(L[i][j] + sum_{j<k<i} L[i][k] X[k][j])
+#pragma unroll
+    for (int dd = 1; dd < kStep; ++dd) {
+        T s = o;
+#pragma unroll
+        for (int kk = 1; kk < dd; ++kk) {
+            const T lik = shfl_c(o, (i + 4 * (j + kk)) & 31), xkj = shfl_c(x, ((j + kk) + 4 * j) & 31);
+            if (i - j == dd) cmac(s, lik, xkj);
+        }
+        if (i - j == dd) x = cmake<R>(-s.x, -s.y);
+    }
+    // inv(U), above: Y[i][j] = -(sum_{i<=k<j} Y[i][k] U[k][j]) / U[j][j]
+#pragma unroll
+    for (int dd = 1; dd < kStep; ++dd) {
+        const T yii = shfl_c(x, 5 * i);
+        T s = cmul(yii, o);
+#pragma unroll
+        for (int kk = 1; kk < dd; ++kk) {
+            const T yik = shfl_c(x, (i + 4 * (i + kk)) & 31), ukj = shfl_c(o, ((i + kk) + 4 * j) & 31);
+            if (j - i == dd) cmac(s, yik, ukj);
+        }
+        if (j - i == dd) x = cmul(cmake<R>(-s.x, -s.y), dj);
+    }
+    if (mine) B[i + j * LD] = x;
+}
+
+// One step of the register-tile build of k_dense_lu (80-row fronts, tile
+// of 5 x 5 entries a thread: rows tx + 16 i, columns ty + 16 j): the rank-kw
+// update with the step's L21 columns and U12 rows read from D, on the tile
+// blocks from ILO = b1 / 16 on, then the next step's panel -- columns [b1,
+// b1 + n1) from row b1 down, rows [b1, b1 + n1) right of them, all inside
+// block ILO -- written back to D (rt_publish).
+template <int ILO, typename T, int TI>
+__device__ __forceinline__ void rt_step(T (&t)[TI][TI], const T *D, int LD, int c0, int kw, int b1, int tx,
+                                        int ty) {
+#pragma unroll
+    for (int k = 0; k < kStep; ++k) {
+        if (k >= kw) break;
+        T l[TI];
+#pragma unroll
+        for (int i = ILO; i < TI; ++i) {
+            const int r = tx + 16 * i;
+            l[i] = r >= b1 ? D[r + (c0 + k) * LD] : czero<T>();
+        }
+#pragma unroll
+        for (int j = ILO; j < TI; ++j) {
+            const int c = ty + 16 * j;
+            const T u = c >= b1 ? D[(c0 + k) + c * LD] : czero<T>();
+#pragma unroll
+            for (int i = ILO; i < TI; ++i) cmsub(t[i][j], l[i], u);
+        }
+    }
+}
+template <int ILO, typename T, int TI>
+__device__ __forceinline__ void rt_publish(const T (&t)[TI][TI], T *D, int LD, int b1, int n1, int tx, int ty) {
+    if (ILO >= TI) return;
+    const int cp = ty + 16 * ILO, rp = tx + 16 * ILO;
+    if (cp >= b1 && cp < b1 + n1) {
+#pragma unroll
+        for (int i = ILO; i < TI; ++i) {
+            const int r = tx + 16 * i;
+            if (r >= b1) D[r + cp * LD] = t[i][ILO];
+        }
+    }
+    if (rp >= b1 && rp < b1 + n1) {
+#pragma unroll
+        for (int j = ILO; j < TI; ++j) {
+            const int c = ty + 16 * j;
+            if (c >= b1 + n1) D[rp + c * LD] = t[ILO][j];
+        }
+    }
 }
 
 // complex64: at most 80 registers so that three CTAs share an SM (the
@@ -406,9 +521,28 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     __syncthreads();
 
     const int tx = tid & 15, ty = tid >> 4;
+    // RT (complex64 fronts padded to 80, the leaves and the fronts of
+    // their parents' level): the trailing matrix stays in registers between
+    // steps -- thread (tx, ty) owns rows tx + 16 i and columns ty + 16 j, a
+    // 5 x 5 tile -- and only the next step's panel column and row go back
+    // to shared memory, instead of a shared-memory read-modify-write of
+    // every updated entry per step.  Same operations in the same order.
+    constexpr bool RT = SC == 80 && sizeof(T) == 8;
+    constexpr int TI = RT ? SC / 16 : 1;
+    T t[TI][TI];
+    if (RT) {
+#pragma unroll
+        for (int i = 0; i < TI; ++i)
+#pragma unroll
+            for (int j = 0; j < TI; ++j) t[i][j] = D[(tx + 16 * i) + (ty + 16 * j) * LD];
+    }
     for (int c0 = 0; c0 < P; c0 += kStep) {
         const int kw = min(kStep, P - c0), b1 = c0 + kw;
-        if (tid == 0) lu4_inv<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
+        if (RT) {
+            if (warp == 0) lu4_inv_warp<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count, lane);
+        } else if (tid == 0) {
+            lu4_inv<T, R>(D + c0 + c0 * LD, LD, kw, tiny, tiny_count);
+        }
         __syncthreads();
         // L21 rows [b1, S): l = a inv(U11) (threads 0-127);  U12 columns
         // [b1, S): u = inv(L11) a (threads 128-255), so each warp runs one
@@ -445,6 +579,23 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
         }
         (void)nr;
         __syncthreads();
+        if constexpr (RT) {
+            // register tiles from the first 16-block still live (b1 / 16, the
+            // same on every thread) on; rows / columns of that block before
+            // b1 take zero multipliers.  The update reads only column and
+            // row c0 + k of D, the next panel lies in columns and rows from
+            // b1 on: no barrier between the two.
+            const int n1 = min(kStep, P - b1);
+            switch (b1 >> 4) {
+            case 0: rt_step<0>(t, D, LD, c0, kw, b1, tx, ty); rt_publish<0>(t, D, LD, b1, n1, tx, ty); break;
+            case 1: rt_step<1>(t, D, LD, c0, kw, b1, tx, ty); rt_publish<1>(t, D, LD, b1, n1, tx, ty); break;
+            case 2: rt_step<2>(t, D, LD, c0, kw, b1, tx, ty); rt_publish<2>(t, D, LD, b1, n1, tx, ty); break;
+            case 3: rt_step<3>(t, D, LD, c0, kw, b1, tx, ty); rt_publish<3>(t, D, LD, b1, n1, tx, ty); break;
+            default: rt_step<4>(t, D, LD, c0, kw, b1, tx, ty); rt_publish<4>(t, D, LD, b1, n1, tx, ty); break;
+            }
+            __syncthreads();
+            continue;
+        }
         // trailing rows / columns [b1, S) -= L21 U12 (rank kw).  Rows and
         // columns of the 16-blocks that lie before b1 take zero multipliers,
         // so their read-modify-write leaves them unchanged and the entry loop
@@ -482,6 +633,17 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
         __syncthreads();
     }
 
+    if constexpr (RT) {
+        // the update matrix (rows and columns from P on) back to shared memory
+#pragma unroll
+        for (int i = 0; i < TI; ++i)
+#pragma unroll
+            for (int j = 0; j < TI; ++j) {
+                const int r = tx + 16 * i, c = ty + 16 * j;
+                if (r >= P && c >= P) D[r + c * LD] = t[i][j];
+            }
+        __syncthreads();
+    }
     // off-diagonal blocks of the inverses over the P x P pivot block, 4
     // rows (columns) at a time.  Thread (col, quarter) of the lower part:
     // T[i] = L[b0+i][col] + sum_{k in (col, b0), k = quarter mod 4} L[b0+i][k] X[k][col]
