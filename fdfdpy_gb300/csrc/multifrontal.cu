@@ -521,13 +521,14 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     __syncthreads();
 
     const int tx = tid & 15, ty = tid >> 4;
-    // RT (complex64 fronts padded to 80, the leaves and the fronts of
-    // their parents' level): the trailing matrix stays in registers between
-    // steps -- thread (tx, ty) owns rows tx + 16 i and columns ty + 16 j, a
-    // 5 x 5 tile -- and only the next step's panel column and row go back
-    // to shared memory, instead of a shared-memory read-modify-write of
-    // every updated entry per step.  Same operations in the same order.
-    constexpr bool RT = SC == 80 && sizeof(T) == 8;
+    // RT (complex64 blocks padded to 80 or 64: the leaves, the fronts of the
+    // levels above them, the panel diagonal blocks): the trailing matrix
+    // stays in registers between steps -- thread (tx, ty) owns rows tx + 16 i
+    // and columns ty + 16 j, a 5 x 5 or 4 x 4 tile -- and only the next
+    // step's panel column and row go back to shared memory, instead of a
+    // shared-memory read-modify-write of every updated entry per step.  Same
+    // operations in the same order.
+    constexpr bool RT = (SC == 80 || SC == 64) && sizeof(T) == 8;
     constexpr int TI = RT ? SC / 16 : 1;
     T t[TI][TI];
     if (RT) {
