@@ -988,6 +988,30 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
     }
 }
 
+// Forward gather of one front into ws (nrhs x ld_ws): w = b on the pivots
+// (zero on the boundary), plus child 0's update, plus child 1's, added in
+// that order; inv0 / inv1 give each of the front's rows its row in the
+// children's update blocks (or -1).  Threads t, t + nt, ... of the caller.
+template <typename T>
+__device__ __forceinline__ void gather_front(const FrontD *__restrict__ fr, const FrontD &f,
+                                             const int32_t *__restrict__ v, const int32_t *__restrict__ inv0,
+                                             const int32_t *__restrict__ inv1, const double2 *__restrict__ b,
+                                             const T *W, int64_t sum_m, int64_t n, int nrhs, T *ws, int ld_ws, int t,
+                                             int nt) {
+    const int64_t u0 = f.c0 >= 0 ? (int64_t)fr[f.c0].voff + fr[f.c0].p : 0;
+    const int64_t u1 = f.c1 >= 0 ? (int64_t)fr[f.c1].voff + fr[f.c1].p : 0;
+    for (int k = t; k < f.m; k += nt) {
+        const int a0 = f.c0 >= 0 ? inv0[f.voff + k] : -1, a1 = f.c1 >= 0 ? inv1[f.voff + k] : -1;
+        const int var = k < f.p ? v[k] : 0;
+        for (int r = 0; r < nrhs; ++r) {
+            T w = (k < f.p) ? from_c128<T>(b[r * n + var], 1.0) : czero<T>();
+            if (a0 >= 0) w = cadd(w, W[r * sum_m + u0 + a0]);
+            if (a1 >= 0) w = cadd(w, W[r * sum_m + u1 + a1]);
+            ws[r * ld_ws + k] = w;
+        }
+    }
+}
+
 // ---- substitutions of levels whose fronts have at most 64 pivots --------------
 // One CTA per front does the whole step of a direction (the gather, the
 // triangular product with the stored inverse and the update rows), instead
@@ -1034,7 +1058,8 @@ __device__ __forceinline__ void rows_dot(const T *F, int64_t ld, int row0, int n
 
 template <typename T>
 __global__ void __launch_bounds__(kSmallThreads)
-    k_fwd_small(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+    k_fwd_small(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0,
+                const int32_t *__restrict__ inv1,
                 const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
                 int nrhs, int f_begin, int maxm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1044,22 +1069,8 @@ __global__ void __launch_bounds__(kSmallThreads)
     const FrontD f = fr[f_begin + blockIdx.x];
     const int32_t *v = vars + f.voff;
     const int tid = threadIdx.x;
-    for (int r = 0; r < nrhs; ++r)
-        for (int k = tid; k < f.m; k += blockDim.x)
-            ws[r * maxm + k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+    gather_front(fr, f, v, inv0, inv1, b, W, sum_m, n, nrhs, ws, maxm, tid, blockDim.x);
     __syncthreads();
-    for (int slot = 0; slot < 2; ++slot) {
-        const int c = slot ? f.c1 : f.c0;
-        if (c < 0) continue;
-        const FrontD ch = fr[c];
-        const int mu = ch.m - ch.p;
-        const int32_t *rm = relmap + ch.voff + ch.p;
-        for (int r = 0; r < nrhs; ++r) {
-            const T *wc = W + r * sum_m + ch.voff + ch.p;
-            for (int a = tid; a < mu; a += blockDim.x) ws[r * maxm + rm[a]] = cadd(ws[r * maxm + rm[a]], wc[a]);
-        }
-        __syncthreads();
-    }
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
     for (int r = 0; r < nrhs; ++r) {
@@ -1214,7 +1225,8 @@ __device__ __forceinline__ void warp_bwd_blocked(const T *F, int64_t ld, int p, 
 
 template <typename T>
 __global__ void __launch_bounds__(32 * kWarpFronts, 4)
-    k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+    k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0,
+               const int32_t *__restrict__ inv1,
                const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
                int nrhs, int f_begin, int nfl, int maxm, int blocked) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1225,21 +1237,8 @@ __global__ void __launch_bounds__(32 * kWarpFronts, 4)
     const FrontD f = fr[f_begin + fi];
     const int32_t *v = vars + f.voff;
     const int p = f.p, m = f.m;
-    for (int r = 0; r < nrhs; ++r)
-        for (int k = lane; k < m; k += 32) ws[r * maxm + k] = (k < p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
+    gather_front(fr, f, v, inv0, inv1, b, W, sum_m, n, nrhs, ws, maxm, lane, 32);
     __syncwarp();
-    for (int slot = 0; slot < 2; ++slot) {
-        const int c = slot ? f.c1 : f.c0;
-        if (c < 0) continue;
-        const FrontD ch = fr[c];
-        const int mu = ch.m - ch.p;
-        const int32_t *rm = relmap + ch.voff + ch.p;
-        for (int r = 0; r < nrhs; ++r) {
-            const T *wc = W + r * sum_m + ch.voff + ch.p;
-            for (int a = lane; a < mu; a += 32) ws[r * maxm + rm[a]] = cadd(ws[r * maxm + rm[a]], wc[a]);
-        }
-        __syncwarp();
-    }
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
     const int r0 = lane, r1 = lane + 32;
@@ -2267,42 +2266,35 @@ __device__ __forceinline__ T diag_rows(const T *Ds, const T *vr, int rn, int row
 template <typename T, typename R, int NR>
 __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
-                const int32_t *__restrict__ vars, const int32_t *__restrict__ relmap,
+                const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0, const int32_t *__restrict__ inv1,
                 const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
                 int *err, const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
     if (NR == 1) nrhs = 1;  // one right-hand side: the sums stay in registers
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    // gather: right-hand side of the pivots and the children's updates; the
-    // pivot slots of Y are marked unpublished
-    for (int fi = blockIdx.x; fi < nfl; fi += gridDim.x) {
+    // gather, spread over every CTA (one entry a thread): w = b on the
+    // pivots (zero on the boundary), plus child 0's update, plus child 1's
+    // -- the inverse maps give each parent row its children's update rows --
+    // added in that order; the pivot slots of Y are marked unpublished
+    const int gchunks = (maxm + (int)blockDim.x - 1) / (int)blockDim.x;
+    for (int item = blockIdx.x; item < nfl * gchunks; item += gridDim.x) {
+        const int fi = item / gchunks, k = (item - fi * gchunks) * (int)blockDim.x + tid;
         const FrontD f = fr[fb + fi];
-        const int32_t *v = vars + f.voff;
+        if (k >= f.m) continue;
+        const int a0 = f.c0 >= 0 ? inv0[f.voff + k] : -1, a1 = f.c1 >= 0 ? inv1[f.voff + k] : -1;
+        const int64_t o0 = a0 >= 0 ? (int64_t)fr[f.c0].voff + fr[f.c0].p + a0 : 0;
+        const int64_t o1 = a1 >= 0 ? (int64_t)fr[f.c1].voff + fr[f.c1].p + a1 : 0;
+        const int var = k < f.p ? vars[f.voff + k] : 0;
         for (int r = 0; r < nrhs; ++r) {
-            T *w = W + r * sum_m + f.voff;
-            for (int k = tid; k < f.m; k += blockDim.x) {
-                w[k] = (k < f.p) ? from_c128<T>(b[r * n + v[k]], 1.0) : czero<T>();
-                if (k < f.p) set_unset(Y + r * sum_m + f.voff + k);
-            }
-        }
-        __syncthreads();
-        for (int slot = 0; slot < 2; ++slot) {
-            const int c = slot ? f.c1 : f.c0;
-            if (c < 0) continue;
-            const FrontD ch = fr[c];
-            const int mu = ch.m - ch.p;
-            const int32_t *rm = relmap + ch.voff + ch.p;
-            for (int r = 0; r < nrhs; ++r) {
-                T *w = W + r * sum_m + f.voff;
-                const T *wc = W + r * sum_m + ch.voff + ch.p;
-                for (int a = tid; a < mu; a += blockDim.x) w[rm[a]] = cadd(w[rm[a]], wc[a]);
-            }
-            __syncthreads();
+            T v = (k < f.p) ? from_c128<T>(b[r * n + var], 1.0) : czero<T>();
+            if (a0 >= 0) v = cadd(v, W[r * sum_m + o0]);
+            if (a1 >= 0) v = cadd(v, W[r * sum_m + o1]);
+            W[r * sum_m + f.voff + k] = v;
+            if (k < f.p) set_unset(Y + r * sum_m + f.voff + k);
         }
     }
     if (!grid_sync(gb, err, bar_limit)) return;
     (void)maxp;
-    (void)maxm;
     // pipelined panels: unit (front, row block R); a pivot block computes
     // y_R = inv(L_RR) (w_R - sum_k L[R, k] y_k) and publishes it, an update
     // block accumulates w_B -= sum_k L[B, k] y_k for the parent's gather
@@ -2506,8 +2498,9 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             const int2 *units = fac->d_units + fac->unit_fwd_off[L];
             int nunits = fac->unit_fwd_n[L];
             unsigned bar_limit = bar_limit_of(fac), flag_limit = flag_limit_of(fac);
+            const int32_t *inv0 = fac->d_inv, *inv1 = fac->d_inv + S.sum_m;
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
-                            (void *)&pool, (void *)&fac->d_vars, (void *)&fac->d_relmap, (void *)&b, (void *)&W,
+                            (void *)&pool, (void *)&fac->d_vars, (void *)&inv0, (void *)&inv1, (void *)&b, (void *)&W,
                             (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err,
                             (void *)&units, (void *)&nunits, (void *)&bar_limit, (void *)&flag_limit};
             // grid: the most work items any phase of this level has, capped
@@ -2522,14 +2515,15 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         if (warp_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
-                            st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, nfl,
-                                  maxm, (int)fac->blocked_level[L]);
+                            st>>>(fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, W, Y, sum_m,
+                                  n, nrhs, fb, nfl, maxm, (int)fac->blocked_level[L]);
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
         if (small_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_small<T><<<nfl, kSmallThreads, small_smem_bytes<T>(nrhs, maxm), st>>>(
-                fac->d_fronts, fac->d_vars, fac->d_relmap, pool, b, W, Y, sum_m, n, nrhs, fb, maxm);
+                fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, W, Y, sum_m, n, nrhs, fb,
+                maxm);
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
