@@ -905,6 +905,19 @@ __device__ __forceinline__ void gemm_tile(const FrontD *__restrict__ fr, T *pool
                     tc_store_b(hi, hi + kBTileBytes, l, cc - ct * kTileNc, v);
                 }
             }
+            // a narrow tile (panels of at most 32 pivots) covers panel rows
+            // [0, 16 QA); the packed rows after it are zero too
+#pragma unroll
+            for (int qa = QA; qa < 4; ++qa) {
+                const int l = ty + 16 * qa;
+#pragma unroll
+                for (int qb = 0; qb < QB; ++qb) {
+                    const int c = cbase + tx + 16 * qb, cc = c - t0, ct = cc / kTileNc;
+                    if (ct >= cts) continue;
+                    uint8_t *hi = bpack + (size_t)ct * 2 * kBTileBytes;
+                    tc_store_b(hi, hi + kBTileBytes, l, cc - ct * kTileNc, czero<c64>());
+                }
+            }
         }
     }
 }
@@ -922,16 +935,19 @@ __global__ void __launch_bounds__(256) k_schur_simt(const FrontD *__restrict__ f
 // HALF: 32-row (L) / 32-column (U) tiles, twice the CTAs, for levels with
 // few fronts whose triangular updates would not fill the GPU.
 // Q = 4, 2 or 1: output tiles of 16 Q rows (L21) / 16 Q columns (U12).
-template <typename T, typename R, int Q>
+// QW = 4 or 2: the panel's side of the tiles, 64 or (panels of at most 32
+// pivots: the single-panel fronts of the levels above the leaves) 32 wide,
+// so that those panels compute no zero columns (rows).
+template <typename T, typename R, int Q, int QW>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_trsm_panel(const FrontD *__restrict__ fr, T *pool, int f_begin, int k0,
                                                     const TcFront *__restrict__ tcf, uint8_t *scratch) {
     __shared__ T As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
     if (blockIdx.z == 0) {
-        gemm_tile<T, R, TRSM_L, Q, 4>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
+        gemm_tile<T, R, TRSM_L, Q, QW>(fr, pool, f_begin, k0, blockIdx.y, 0, As, Bs);
     } else {
         uint8_t *bpack = tcf ? scratch + tcf[f_begin + blockIdx.x].b_off : nullptr;
-        gemm_tile<T, R, TRSM_U, 4, Q>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
+        gemm_tile<T, R, TRSM_U, QW, Q>(fr, pool, f_begin, k0, 0, blockIdx.y, As, Bs, bpack);
     }
 }
 
@@ -939,19 +955,28 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 3 : 1) k_trsm_panel(cons
 // upper bound of m - t0).  Half-height tiles while the level would launch
 // fewer than 1024 CTAs, quarter-height ones below 256 (the last panels of the
 // few large fronts near the root, on the factorization's critical path).
-template <typename T, typename R>
-void trsm_launch(int nfl, int trail, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0,
-                 const TcFront *tcf, uint8_t *scratch) {
+template <typename T, typename R, int QW>
+void trsm_launch_w(int nfl, int trail, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0,
+                   const TcFront *tcf, uint8_t *scratch) {
     const int tiles = (trail + BM - 1) / BM;
     if (nfl * tiles * 2 < 256) {
         const int t4 = (trail + BM / 4 - 1) / (BM / 4);
-        k_trsm_panel<T, R, 1><<<dim3(nfl, t4, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+        k_trsm_panel<T, R, 1, QW><<<dim3(nfl, t4, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     } else if (nfl * tiles * 2 < 1024) {
         const int t2 = (trail + BM / 2 - 1) / (BM / 2);
-        k_trsm_panel<T, R, 2><<<dim3(nfl, t2, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+        k_trsm_panel<T, R, 2, QW><<<dim3(nfl, t2, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     } else {
-        k_trsm_panel<T, R, 4><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
+        k_trsm_panel<T, R, 4, QW><<<dim3(nfl, tiles, 2), 256, 0, st>>>(fr, pool, fb, k0, tcf, scratch);
     }
+}
+// maxw: the level's widest panel at k0 (min(64, max p - k0))
+template <typename T, typename R>
+void trsm_launch(int nfl, int trail, int maxw, cudaStream_t st, const FrontD *fr, T *pool, int fb, int k0,
+                 const TcFront *tcf, uint8_t *scratch) {
+    if (maxw <= NB / 2)
+        trsm_launch_w<T, R, 2>(nfl, trail, st, fr, pool, fb, k0, tcf, scratch);
+    else
+        trsm_launch_w<T, R, 4>(nfl, trail, st, fr, pool, fb, k0, tcf, scratch);
 }
 
 // ---- solve ------------------------------------------------------------------
@@ -1858,7 +1883,8 @@ int factor_level_lookahead(fdfd_factor *fac, int fb, int nfl, int maxm, int maxp
         const int trail = maxm - k0 - 1;  // upper bound of m - t0
         if (trail <= 0) continue;
         prof_begin(PROF_TRSM, st);
-        trsm_launch<T, R>(nfl, trail, st, fac->d_fronts, pool, fb, k0, fac->d_tcf, fac->d_scratch);
+        trsm_launch<T, R>(nfl, trail, std::min(NB, maxp - k0), st, fac->d_fronts, pool, fb, k0, fac->d_tcf,
+                          fac->d_scratch);
         prof_end(PROF_TRSM, st, 1);
         prof_begin(PROF_SCHUR, st);
         int rc = FDFD_OK;
@@ -1962,8 +1988,8 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
             if (trail <= 0) continue;
             const int tiles = (trail + BM - 1) / BM;
             prof_begin(PROF_TRSM, st);
-            trsm_launch<T, R>(nfl, trail, st, fac->d_fronts, pool, fb, k0, tc ? fac->d_tcf : nullptr,
-                              tc ? fac->d_scratch : nullptr);
+            trsm_launch<T, R>(nfl, trail, std::min(NB, maxp - k0), st, fac->d_fronts, pool, fb, k0,
+                              tc ? fac->d_tcf : nullptr, tc ? fac->d_scratch : nullptr);
             prof_end(PROF_TRSM, st, 1);
             if (tc) {
                 prof_begin(PROF_SCHUR, st);
