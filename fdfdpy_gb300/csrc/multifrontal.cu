@@ -1248,8 +1248,11 @@ __device__ __forceinline__ void warp_bwd_blocked(const T *F, int64_t ld, int p, 
     __syncwarp();
 }
 
+// complex64: at most 48 (forward) / 40 (backward) registers, so that 40 / 48
+// warps stay resident on an SM -- the passes wait on their loads (long
+// scoreboard), and more warps keep more of them in flight.
 template <typename T>
-__global__ void __launch_bounds__(32 * kWarpFronts, 4)
+__global__ void __launch_bounds__(32 * kWarpFronts, sizeof(T) == 8 ? 5 : 4)
     k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0,
                const int32_t *__restrict__ inv1,
                const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
@@ -1311,7 +1314,7 @@ __global__ void __launch_bounds__(32 * kWarpFronts, 4)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kWarpFronts, 4)
+__global__ void __launch_bounds__(32 * kWarpFronts, sizeof(T) == 8 ? 6 : 4)
     k_bwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const T *__restrict__ pool,
                const T *__restrict__ Y, double2 *x, int64_t sum_m, int64_t n, int nrhs, int f_begin, int nfl,
                int maxm, int blocked) {
