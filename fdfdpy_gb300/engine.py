@@ -296,7 +296,17 @@ class Factor:
                     cur.wait_event(ev)
         if h is None:
             h = C.c_void_p()
-            N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
+            try:
+                N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
+            except N.FDFDError as e:
+                if e.code != N.FDFD_ERR_OOM:
+                    raise
+                # parked factors (and torch's cached blocks) are caches: free
+                # them and try once more before reporting the shortage
+                release_cached_factors()
+                torch.cuda.empty_cache()
+                h = C.c_void_p()
+                N.call("fdfd_factor_create", sym.handle, N.PREC[precision], self.max_nrhs, C.byref(h))
         self.handle = h
         N.call("fdfd_factor_set_pivot_tol", h, -1.0 if pivot_tol is None else float(pivot_tol))
         N.call("fdfd_factor_set_fused_limit", h, -1 if fused_max_m is None else int(fused_max_m))

@@ -148,54 +148,63 @@ class SolveServer:
         return self.resident + need <= self.budget
 
     # ---- one unit of work (a cache hit or a batch of misses) on one stream -----
-    def _serve(self, reqs, stream, t0, pinned):
+    def _serve(self, reqs, stream, t0, pinned, need=0):
         start = time.perf_counter() - t0
         for r in reqs:
             r.start = start
-        with torch.cuda.stream(stream):
-            if pinned is not None:
-                eid, pos = pinned
-                ent = self.cache[eid]
-                reqs[0].cache_hit = True
-                positions = [pos]
-            else:
-                ops = [engine.DeviceOperator(r.omega, r.eps_r, r.eps_r.shape[0] * r.dl, r.eps_r.shape[1] * r.dl,
-                                             r.NPML, r.pol, r.L0) for r in reqs]
-                B = len(reqs)
-                shape = reqs[0].eps_r.shape
-                if B > 1:
-                    fac = engine.BatchFactor(self._sym(shape, B), self.precision, max_nrhs=8,
-                                             fused_max_m=self._fused(shape))
-                    fac.numeric(ops)
+        ent = eid = None
+        try:
+            with torch.cuda.stream(stream):
+                if pinned is not None:
+                    eid, pos = pinned
+                    ent = self.cache[eid]
+                    reqs[0].cache_hit = True
+                    positions = [pos]
                 else:
-                    fac = engine.Factor(self._sym(shape), self.precision, max_nrhs=8,
-                                        fused_max_m=self._fused(shape)).numeric(ops[0])
-                with self.cv:
-                    self.factorizations += 1
-                eid = next(self._ids)
-                ent = _CacheEntry(ops, fac, self._need(reqs[0].eps_r.shape, B), [r.key for r in reqs], users=1)
-                positions = list(range(B))
-            ent.lock.acquire()
-            try:
-                self._solve_on(ent, reqs, positions)
-            finally:
-                # work queued on this stream may still use the factor's solve
-                # workspace: it must finish before another stream takes the factor
+                    ops = [engine.DeviceOperator(r.omega, r.eps_r, r.eps_r.shape[0] * r.dl,
+                                                 r.eps_r.shape[1] * r.dl, r.NPML, r.pol, r.L0) for r in reqs]
+                    B = len(reqs)
+                    shape = reqs[0].eps_r.shape
+                    if B > 1:
+                        fac = engine.BatchFactor(self._sym(shape, B), self.precision, max_nrhs=8,
+                                                 fused_max_m=self._fused(shape))
+                        fac.numeric(ops)
+                    else:
+                        fac = engine.Factor(self._sym(shape), self.precision, max_nrhs=8,
+                                            fused_max_m=self._fused(shape)).numeric(ops[0])
+                    with self.cv:
+                        self.factorizations += 1
+                    eid = next(self._ids)
+                    ent = _CacheEntry(ops, fac, need, [r.key for r in reqs], users=1)
+                    positions = list(range(B))
+                ent.lock.acquire()
                 try:
-                    stream.synchronize()
+                    self._solve_on(ent, reqs, positions)
                 finally:
-                    ent.lock.release()
+                    # work queued on this stream may still use the factor's solve
+                    # workspace: it must finish before another stream takes the factor
+                    try:
+                        stream.synchronize()
+                    finally:
+                        ent.lock.release()
+        except Exception as e:  # e.g. the factor did not fit: these requests fail, the slot goes on
+            for r in reqs:
+                if r.error is None and r.x is None:
+                    r.error = repr(e)
         with self.cv:
-            ent.users -= 1
-            if pinned is not None:
-                pass                           # a cache hit: stays resident
-            elif ent.bytes <= self.cache_budget:
-                self.cache[eid] = ent          # keep it resident for reuse
-                for p, k in enumerate(ent.keys):
-                    self.key_index.setdefault(k, (eid, p))
+            if ent is None:
+                self.resident -= need          # nothing was built
             else:
-                self.resident -= ent.bytes     # not kept: its memory is released
-                del ent
+                ent.users -= 1
+                if pinned is not None:
+                    pass                       # a cache hit: stays resident
+                elif ent.bytes <= self.cache_budget:
+                    self.cache[eid] = ent      # keep it resident for reuse
+                    for p, k in enumerate(ent.keys):
+                        self.key_index.setdefault(k, (eid, p))
+                else:
+                    self.resident -= ent.bytes  # not kept: its memory is released
+                    ent = None
             self.cv.notify_all()
         done = time.perf_counter() - t0
         for r in reqs:
@@ -310,7 +319,8 @@ class SolveServer:
                         break
                     self.resident += need
                     slot = free_slots.pop()
-                    th = threading.Thread(target=self._serve, args=(group, streams[slot], t0, pinned), daemon=True)
+                    th = threading.Thread(target=self._serve, args=(group, streams[slot], t0, pinned, need),
+                                          daemon=True)
                     th.start()
                     threads.append((th, slot))
                     idx += 1

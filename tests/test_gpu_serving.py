@@ -171,3 +171,31 @@ def test_autotuner_picks_a_measured_candidate(tmp_path):
     reqs = make_stream(n_requests=8, rate=1e6, sides=(96,), reuse=0.0, seed=4, npml=(8, 8))
     s = SolveServer(slots=2, precision="c64", autotune=tuner, batch_max=8).run(reqs, realtime=False)
     assert s["failed"] == 0 and s["max_rel_residual"] <= 1e-10
+
+
+def test_failed_factorization_fails_its_requests_and_the_slot_goes_on(monkeypatch):
+    """A factorization that raises inside a slot (here a simulated device
+    allocation failure, raised on the host for one grid) fails exactly the
+    requests of that unit of work; the slot is freed, the memory it had
+    reserved is returned, and the other requests are served."""
+    from fdfdpy_gb300 import engine, _native as N
+    from fdfdpy_gb300.serving import SolveServer
+    reqs = _requests()[:6]
+    bad_shape = reqs[0].eps_r.shape
+    real_init = engine.Factor.__init__
+
+    def flaky_init(self, sym, *a, **k):
+        if (sym.Nx, sym.Ny) == bad_shape:
+            raise N.FDFDError(N.FDFD_ERR_OOM, "factor_create: device allocation failed")
+        real_init(self, sym, *a, **k)
+
+    monkeypatch.setattr(engine.Factor, "__init__", flaky_init)
+    srv = SolveServer(slots=2, precision="c64", tol=1e-10, batch_max=1, cache_budget=0)
+    s = srv.run(reqs, realtime=False)
+    bad = [r for r in reqs if r.eps_r.shape == bad_shape]
+    good = [r for r in reqs if r.eps_r.shape != bad_shape]
+    assert bad and good
+    assert s["failed"] == len(bad)
+    assert all(r.error and "allocation" in r.error and r.x is None for r in bad)
+    assert all(r.error is None and r.rel_residual <= 1e-10 for r in good)
+    assert srv.resident == 0
