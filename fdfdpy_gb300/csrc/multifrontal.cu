@@ -177,8 +177,12 @@ __global__ void k_extend_pull(const FrontD *__restrict__ fr, const int32_t *__re
     const int32_t *i0 = inv0 + f.voff, *i1 = inv1 + f.voff;
     T *F = pool + f.f_off;
     const int64_t ld = f.ld;
+    // (column, row) of entry idx = bb m + a, advanced by blockDim.x entries
+    // a pass without a division per entry
+    const int step_b = (int)blockDim.x / m, step_a = (int)blockDim.x - step_b * m;
+    int bb = (int)threadIdx.x / m, a = (int)threadIdx.x - bb * m;
     for (int idx = threadIdx.x; idx < cols * m; idx += blockDim.x) {
-        const int bb = idx / m, a = idx - bb * m, b = b0 + bb;
+        const int b = b0 + bb;
         T v = czero<T>();
         if (U0) {
             const int ia = i0[a], ib = i0[b];
@@ -189,6 +193,12 @@ __global__ void k_extend_pull(const FrontD *__restrict__ fr, const int32_t *__re
             if (ia >= 0 && ib >= 0) v = cadd(v, U1[ia + (int64_t)ib * ld1]);
         }
         F[a + (int64_t)b * ld] = v;
+        a += step_a;
+        bb += step_b;
+        if (a >= m) {
+            a -= m;
+            ++bb;
+        }
     }
 }
 
