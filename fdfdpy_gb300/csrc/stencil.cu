@@ -9,7 +9,6 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <mutex>
 
 #include "stencil.cuh"
 
@@ -586,28 +585,18 @@ constexpr int kNoAllocMaxCols = 8;  // columns per call (documented limit)
 constexpr size_t kNoAllocDoubles = (size_t)kNormParts * kNoAllocMaxCols + kNoAllocMaxCols;
 static __device__ __align__(256) double g_norms_scratch[kNoAllocDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-double *g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up
-// once per device (host code may not take the address of a __device__
-// symbol directly: the host-side name is only a stand-in).
+// Device address of the scratch array in the current context (host code
+// may not take the address of a __device__ symbol directly: the host-side
+// name is only a stand-in).  Looked up on every call -- a cheap query, and
+// a cached address would go stale once the context is reset and the module
+// loaded again.
 int noalloc_scratch(double **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(FDFD_ERR_NO_DEVICE, std::string("norms_noalloc: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(FDFD_ERR_BAD_ARG, "norms_noalloc: device index out of range");
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_norms_scratch);
-        if (e != cudaSuccess || !ptr)
-            return fail(FDFD_ERR_CUDA, std::string("norms_noalloc: cudaGetSymbolAddress failed: ") +
-                                           cudaGetErrorString(e));
-        g_scratch_ptr[dev] = (double *)ptr;
-    }
-    *out = g_scratch_ptr[dev];
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_norms_scratch);
+    if (e != cudaSuccess || !ptr)
+        return fail(e == cudaErrorNoDevice ? FDFD_ERR_NO_DEVICE : FDFD_ERR_CUDA,
+                    std::string("norms_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+    *out = (double *)ptr;
     return FDFD_OK;
 }
 }  // namespace

@@ -206,12 +206,11 @@ int fdfd_norms(const void *v, int64_t n, int32_t ncol, double *out_host,
  *   - The scratch is one fixed array in the library's static device memory
  *     (about 39 KB); every GPU that loads the library holds it until exit.
  *   - At most 8 columns per call; more returns FDFD_ERR_BAD_ARG.
- *   - The first call on a device looks up the array's device address (once
- *     per device); make that first call before any stream capture.
  *   - Every call shares the array: calls that overlap on the GPU (other
  *     streams, other threads) race and must be serialised by the caller.
  *   - Never calls cudaMalloc, cudaFree or an allocating library routine;
- *     synchronises the stream to return the result in out_host.          */
+ *     synchronises the stream to return the result in out_host, so it
+ *     cannot be called while the stream is being captured into a graph. */
 int fdfd_norms_noalloc(const void *v, int64_t n, int32_t ncol,
                        double *out_host, void *stream);
 
