@@ -547,21 +547,48 @@ def run_kerr(args):
     amps = np.logspace(2, 5, 8)
     results = {}
 
+    # each thread first runs two Newton steps of a 128^2 problem of the same
+    # kind (library and kernel loading, per-thread handles), then all start
+    # together: the wall clock covers the eight solves only
+    M = 128
+    eps_w = np.ones((M, M))
+    eps_w[44:84, 44:84] = 12
+    region_w = (eps_w > 1).astype(float)
+    start = threading.Barrier(len(amps) + 1)
+
     def one(k, a, stream):
+        try:
+            solve(k, a, stream)
+        except BaseException:
+            start.abort()  # the other threads and the clock do not wait for this one
+            raise
+
+    def solve(k, a, stream):
         with torch.cuda.stream(stream):
+            warm = Simulation(om, eps_w, 0.02, [20, 20], "Ez")
+            warm.precision = args.precision
+            warm.src[25, M // 2] = a
+            warm.add_nl(2.8e-18, region_w)
+            warm.solve_fields_nl(solver_nl="newton", conv_threshold=1e-10, max_num_iter=2)
             sim = Simulation(om, eps, 0.02, [20, 20], "Ez")
             sim.precision = args.precision
             sim.src[N * 200 // 1024, N // 2] = a
             sim.add_nl(2.8e-18, region)
+            torch.cuda.current_stream().synchronize()
+            start.wait(timeout=900)
             t0 = time.perf_counter()
             out = sim.solve_fields_nl(solver_nl="newton", conv_threshold=1e-10, max_num_iter=args.newton_iters)
             results[k] = {"amplitude": float(a), **conv_summary(out[3][:, 0]), "s": time.perf_counter() - t0}
 
     streams = [torch.cuda.Stream() for _ in amps]
-    t0 = time.perf_counter()
     ths = [threading.Thread(target=one, args=(k, a, st)) for k, (a, st) in enumerate(zip(amps, streams))]
     for t in ths:
         t.start()
+    try:
+        start.wait(timeout=900)
+    except threading.BrokenBarrierError:
+        pass  # a thread failed: its traceback goes to stderr, its amplitude is missing below
+    t0 = time.perf_counter()
     for t in ths:
         t.join()
     torch.cuda.synchronize()
