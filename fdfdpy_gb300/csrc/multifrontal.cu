@@ -2418,28 +2418,19 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         }
         __syncthreads();
     }
-    if (!grid_sync(gb, err, bar_limit)) return;
-    // opener, pass 2: acc = y - sum of the column blocks, in a fixed order;
-    // the pivot slots of Y are then marked unpublished (x goes there)
+    // the pivot slots of W (free in the backward pass) become the
+    // publication slots of x: marked unpublished before the grid barrier
     const int prow2 = (maxp + kRowsPerCta - 1) / kRowsPerCta;
     for (int item = blockIdx.x; item < nfl * prow2; item += gridDim.x) {
-        const int fi = item / prow2, rc = item % prow2;
+        const int fi = item / prow2, row = (item % prow2) * kRowsPerCta + tid;
         const FrontD f = fr[fb + fi];
-        const int row = rc * kRowsPerCta + tid;
-        if (row < f.p) {
-            const int nch = (f.m - f.p + kRowsPerCta - 1) / kRowsPerCta;
-            const T *base = scratch + bwd_off[fb + fi];
-            for (int r = 0; r < nrhs; ++r) {
-                T acc = Y[r * sum_m + f.voff + row];
-                for (int c = 0; c < nch; ++c) acc = csub(acc, base[((int64_t)c * nrhs + r) * f.p + row]);
-                W[r * sum_m + f.voff + row] = acc;
-                set_unset(Y + r * sum_m + f.voff + row);
-            }
-        }
+        if (row < f.p)
+            for (int r = 0; r < nrhs; ++r) set_unset(W + r * sum_m + f.voff + row);
     }
     if (!grid_sync(gb, err, bar_limit)) return;
     // pipelined panels, descending: x_R = inv(U_RR) (acc_R - sum_{j>R} U[R, j] x_j),
-    // published in Y's pivot rows (and written to the global solution)
+    // with acc = y - the opener's column blocks (summed in a fixed order);
+    // x published in W's pivot rows (and written to the global solution)
     T *Ds = xs, *vin = xs + NB * NB;
     const int rr = tid >> 2, q = tid & 3;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
@@ -2451,15 +2442,22 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         const T *F = pool + f.f_off;
         const int64_t ld = f.ld;
         const bool live = rr < rn;
-        // this unit's rows of acc are final since the opener: load them off
-        // the chain between units
+        // this unit's rows of acc, final since the opener: formed off the
+        // chain between units
         T *wpre = vin + nrhs * NB;
-        if (live && q == 0)
-            for (int r = 0; r < nrhs; ++r) wpre[r * NB + rr] = ldcg_c(W + r * sum_m + f.voff + r0 + rr);
+        if (live && q == 0) {
+            const int nch = (f.m - f.p + kRowsPerCta - 1) / kRowsPerCta;
+            const T *base = scratch + bwd_off[fb + fi];
+            for (int r = 0; r < nrhs; ++r) {
+                T a = Y[r * sum_m + f.voff + r0 + rr];
+                for (int c = 0; c < nch; ++c) a = csub(a, base[((int64_t)c * nrhs + r) * f.p + r0 + rr]);
+                wpre[r * NB + rr] = a;
+            }
+        }
         stage_diag<T, true>(F, ld, r0, rn, Ds);
         T acc[NR];
         for (int r = 0; r < nrhs; ++r) acc[r] = czero<T>();
-        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, Y + f.voff, sum_m, nrhs, err, flag_limit, vin,
+        if (!unit_panels(F, ld, r0, live, KP - 1, rb, -1, f.p, W + f.voff, sum_m, nrhs, err, flag_limit, vin,
                          acc))
             return;
         quad_reduce(acc, nrhs);
@@ -2470,7 +2468,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         for (int r = 0; r < nrhs; ++r) {
             const T xv = diag_rows<T, true>(Ds, vin + r * NB, rn, rr);
             if (live && q == 0) {
-                put_value(Y + r * sum_m + f.voff + r0 + rr, xv);
+                put_value(W + r * sum_m + f.voff + r0 + rr, xv);
                 x[r * n + v[rr]] = to_c128(xv, 1.0);
             }
         }
