@@ -660,16 +660,14 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
     // T[i] = L[b0+i][col] + sum_{k in (col, b0), k = quarter mod 4} L[b0+i][k] X[k][col]
     const int nb4 = (P + kStep - 1) / kStep;
     const int q = tid & 3, g = tid >> 2;  // 64 groups of four threads
-    for (int B = 1; B < nb4; ++B) {
-        const int b0 = B * kStep, bs = min(kStep, P - b0);
-        // blocked: only columns (rows) of b0's 16-block take part
-        const int glo = blocked ? (b0 & ~15) : 0;
-        if (glo == b0) continue;
+    // one 4-row block b0 of both inverses; groups with act set take column
+    // (row) g.  Every thread runs the shuffles and the two barriers.
+    auto complete = [&](int b0, int bs, bool act) {
         T vl[kStep], vu[kStep];
         // lower: groups g < b0 take column g; upper: groups g < b0 take row g
 #pragma unroll
         for (int i = 0; i < kStep; ++i) vl[i] = vu[i] = czero<T>();
-        if (g < b0 && g >= glo) {
+        if (act) {
             const int col = g;
             for (int k = col + 1 + q; k < b0; k += 4) {
                 const T x = D[k + col * LD];
@@ -693,7 +691,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
             }
         // X[B, col] = -inv(L_BB) (L[B, col] + sum), Y[row, B] = -(sum) inv(U_BB)
         T xo[kStep], yo[kStep];
-        if (g < b0 && g >= glo && q == 0) {
+        if (act && q == 0) {
             const int col = g;
 #pragma unroll
             for (int i = 0; i < kStep; ++i)
@@ -714,7 +712,7 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
             }
         }
         __syncthreads();
-        if (g < b0 && g >= glo && q == 0) {
+        if (act && q == 0) {
             const int col = g, row = g;
 #pragma unroll
             for (int i = 0; i < kStep; ++i)
@@ -724,6 +722,20 @@ __global__ void __launch_bounds__(kDenseThreads, sizeof(T) == 8 ? 3 : 1) k_dense
                 }
         }
         __syncthreads();
+    };
+    if (blocked) {
+        // only inside 16 x 16 diagonal blocks, which are independent: block
+        // s of every 16-block at once (group g belongs to the 16-block of
+        // column g, the same for the 16 groups of two warps)
+        for (int sb = 1; sb < 16 / kStep; ++sb) {
+            const int b0 = (g & ~15) + kStep * sb;
+            complete(b0, min(kStep, P - b0), (g & 15) < kStep * sb && b0 < P);
+        }
+    } else {
+        for (int B = 1; B < nb4; ++B) {
+            const int b0 = B * kStep;
+            complete(b0, min(kStep, P - b0), g < b0);
+        }
     }
     for (int c = warp; c < n; c += kDenseThreads / 32)
         for (int r = lane; r < n; r += 32) G[r + (int64_t)c * ld] = D[r + c * LD];
