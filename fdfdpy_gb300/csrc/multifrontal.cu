@@ -82,14 +82,89 @@ struct FrontD {
 // values instead of re-deriving them per cell (and per neighbour for A^T).
 // coef[d * ld + k]: ld = n for one operator, the batch's total for problem
 // b's slice of a batch (coef then points at the slice).
-__global__ void k_coef(OpDev o, double2 *coef, int64_t ld) {
-    const int64_t n = (int64_t)o.Nx * o.Ny;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        double2 c[5];
-        stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
-#pragma unroll
-        for (int d = 0; d < 5; ++d) coef[d * ld + k] = c[d];
+//
+// The values are stencil_row's, bit for bit, with about half of its FP64
+// operations:
+// * a scaling by -1/dx (-1/dy) is the negation of the one by +1/dx (+1/dy)
+//   (rounding to nearest is symmetric), so each product of two negated
+//   factors is the product of the positive ones, the two centre products of
+//   a direction that carry one minus sign are its negated neighbour
+//   coefficients, and the centre is the diagonal term minus
+//   (c_xm + c_xp) + (c_ym + c_yp), summed in stencil_row's order;
+// * every 1/eps_x and 1/eps_y (Hz) serves two cells: a thread walks down its
+//   column carrying 1/eps_x, eps_r and the 1/s_xb factor of the next row,
+//   and a block hands 1/eps_y of each cell to the thread of the previous
+//   column through shared memory.
+// Block: kCoefCols consecutive columns j0 + t over the rows [r0, r1) of one
+// run; grid: (column blocks, row runs), one wave of CTAs where the grid
+// allows, so that every CTA has the same number of rows (+-1).
+constexpr int kCoefCols = 256;
+__global__ void __launch_bounds__(kCoefCols) k_coef(OpDev o, double2 *coef, int64_t ld, int rows_per_run) {
+    __shared__ double s_ty[2][kCoefCols + 1];
+    const int Nx = o.Nx, Ny = o.Ny, t = threadIdx.x;
+    const int j0 = blockIdx.x * kCoefCols, j = j0 + t;
+    const int r0 = blockIdx.y * rows_per_run, r1 = min(r0 + rows_per_run, Nx);
+    if (r0 >= Nx) return;  // block-uniform
+    const bool live = j < Ny;
+    const int jc = live ? j : Ny - 1;  // idle threads of the last column block evaluate a valid cell
+    const int jp = (jc == Ny - 1) ? 0 : jc + 1;
+    const int jm = (jc == 0) ? Ny - 1 : jc - 1;
+    // The one thread of the block whose next column (jp) is not the next
+    // thread's: the last live column (next column 0) or the block's last
+    // thread (next column j0 + kCoefCols); that column is jx.
+    const int te = min(kCoefCols - 1, Ny - 1 - j0);
+    const int jx = (j0 + kCoefCols < Ny) ? j0 + kCoefCols : 0;
+    const bool hz = o.pol == FDFD_POL_HZ;
+    const double vx = o.invdx, vy = o.invdy;
+    double2 fy = c_scale_rn(o.isyf[jc], vy);
+    if (!hz) fy = c_scale_rn(fy, o.invmu);  // (Dyf * 1 / MU_0_)
+    const double2 by0 = c_scale_rn(o.isyb[jc], vy), by1 = c_scale_rn(o.isyb[jp], vy);
+    double2 bx0 = c_scale_rn(o.isxb[r0], vx);
+    double e0 = eps_e(o, r0, jc);
+    double tx0 = hz ? inv_eps_x(o, r0, jc) : 0.0;
+    int buf = 0;
+    for (int i = r0; i < r1; ++i) {
+        const int ip = (i == Nx - 1) ? 0 : i + 1;
+        double2 fx = c_scale_rn(o.isxf[i], vx);
+        if (!hz) fx = c_scale_rn(fx, o.invmu);
+        const double2 bx1 = c_scale_rn(o.isxb[ip], vx);
+        const double e1 = eps_e(o, ip, jc);
+        double2 c1, c2, c3, c4, diag;
+        if (hz) {
+            // inv_eps_x(ip, j): the row below ip's is i; inv_eps_y(i, j)
+            const double tx1 = __ddiv_rn(1.0, o.averaging ? __dmul_rn(__dadd_rn(e0, e1), 0.5) : e1);
+            const double ty0 = __ddiv_rn(1.0, o.averaging ? __dmul_rn(__dadd_rn(eps_e(o, i, jm), e0), 0.5) : e0);
+            s_ty[buf][t] = ty0;
+            if (t == kCoefCols - 1) s_ty[buf][kCoefCols] = inv_eps_y(o, i, jx);
+            __syncthreads();
+            const double ty1 = s_ty[buf][t == te ? kCoefCols : t + 1];  // inv_eps_y(i, jp)
+            buf ^= 1;  // the next row writes the other buffer; the one after passes this row's barrier first
+            c1 = c_mul_rn(c_scale_rn(fx, tx0), bx0);
+            c2 = c_mul_rn(c_scale_rn(fx, tx1), bx1);
+            c3 = c_mul_rn(c_scale_rn(fy, ty0), by0);
+            c4 = c_mul_rn(c_scale_rn(fy, ty1), by1);
+            diag = make_double2(o.w2mu, 0.0);
+            tx0 = tx1;
+        } else {
+            c1 = c_mul_rn(fx, bx0);
+            c2 = c_mul_rn(fx, bx1);
+            c3 = c_mul_rn(fy, by0);
+            c4 = c_mul_rn(fy, by1);
+            diag = make_double2(__dmul_rn(o.w2, e0), 0.0);
+        }
+        if (live) {
+            const int64_t k = (int64_t)i * Ny + j;
+            double2 ctr = c_sub_rn(diag, c_add_rn(c_add_rn(c1, c2), c_add_rn(c3, c4)));
+            if (o.eps_add) ctr.x = __dadd_rn(ctr.x, __dmul_rn(o.w2e0L, o.eps_add[k]));
+            if (o.diag_add) ctr = c_add_rn(ctr, o.diag_add[k]);
+            coef[k] = ctr;
+            coef[ld + k] = c1;
+            coef[2 * ld + k] = c2;
+            coef[3 * ld + k] = c3;
+            coef[4 * ld + k] = c4;
+        }
+        bx0 = bx1;
+        e0 = e1;
     }
 }
 
@@ -99,9 +174,15 @@ __global__ void k_maxdiag(OpDev o, unsigned long long *out) {
     double mx = 0.0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        double2 c[5];
-        stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
-        mx = fmax(mx, hypot(c[0].x, c[0].y));
+        double2 c0;
+        if (o.stencil) {
+            c0 = o.stencil[k];  // stored coefficients: the centre row of [5][n]
+        } else {
+            double2 c[5];
+            stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
+            c0 = c[0];
+        }
+        mx = fmax(mx, hypot(c0.x, c0.y));
     }
     for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
@@ -1779,6 +1860,17 @@ inline int grid1(int64_t n) {
     return (int)b;
 }
 
+// k_coef over an Nx x Ny operator: column blocks x row runs, the runs sized
+// so that the grid is about `ctas` CTAs (one wave) when the grid has rows
+// enough.
+void coef_launch(const OpDev &o, double2 *coef, int64_t ld, int ctas, cudaStream_t st) {
+    const int ncb = (o.Ny + kCoefCols - 1) / kCoefCols;
+    const int runs = std::max(1, std::min(o.Nx, ctas / ncb));
+    const int rows = (o.Nx + runs - 1) / runs;
+    const dim3 grid(ncb, (o.Nx + rows - 1) / rows);
+    k_coef<<<grid, kCoefCols, 0, st>>>(o, coef, ld, rows);
+}
+
 }  // namespace
 }  // namespace fdfd
 
@@ -1816,6 +1908,7 @@ struct fdfd_factor {
     // cooperative per-level solves (levels with many panel steps)
     std::vector<char> coop_level;
     int coop_grid = 0;
+    int coef_ctas = 152;  // resident k_coef CTAs on the device
     void *d_bar = nullptr;
     int *d_solve_err = nullptr;
     int64_t *d_coop_off = nullptr;
@@ -3038,6 +3131,14 @@ extern "C" int fdfd_factor_create(fdfd_symbolic *sym, int32_t precision, int32_t
         rc = (precision != FDFD_PREC_C128) ? coop_grid_for<c64, float>(max_nrhs, &f->coop_grid)
                                            : coop_grid_for<c128, double>(max_nrhs, &f->coop_grid);
         if (rc == FDFD_OK && f->coop_grid == 0) f->coop_level.assign(S.nlev, 0);  // no cooperative launch
+        if (rc == FDFD_OK) {
+            int dev = 0, sms = 0, per_sm = 0;
+            e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_coef, kCoefCols, 0);
+            if (e != cudaSuccess) rc = fail(FDFD_ERR_CUDA, std::string("factor_create: ") + cudaGetErrorString(e));
+            else f->coef_ctas = std::max(1, sms * per_sm);
+        }
         if (rc == FDFD_OK &&
             (!alloc(&f->d_bar, sizeof(GridBar)) || !alloc((void **)&f->d_solve_err, 4) ||
              !alloc((void **)&f->d_coop_off, S.nf * sizeof(int64_t)) || !alloc(&f->d_coop_scratch, ce * f->elem))) {
@@ -3127,7 +3228,7 @@ extern "C" int fdfd_factor_numeric(fdfd_factor *fac, const fdfd_operator *op, vo
     fac->coef_valid = false;
     if (!o.stencil) {
         prof_begin(PROF_ASSEMBLE, st);
-        k_coef<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_coef, fac->n);
+        coef_launch(o, fac->d_coef, fac->n, fac->coef_ctas, st);
         prof_end(PROF_ASSEMBLE, st, 1);
         o.stencil = fac->d_coef;
     }
@@ -3302,7 +3403,7 @@ extern "C" int fdfd_factor_numeric_batch(fdfd_factor *fac, const fdfd_operator *
             return fail(FDFD_ERR_BAD_ARG, "factor_numeric_batch: operator " + std::to_string(b) +
                                               " differs from the batch's grid");
         prof_begin(PROF_ASSEMBLE, st);
-        k_coef<<<grid1(n1), 256, 0, st>>>(o, fac->d_coef + b * n1, fac->n);
+        coef_launch(o, fac->d_coef + b * n1, fac->n, fac->coef_ctas, st);
         prof_end(PROF_ASSEMBLE, st, 1);
     }
     fac->has_p = false;
