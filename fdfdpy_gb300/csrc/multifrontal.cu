@@ -1116,15 +1116,16 @@ __global__ void k_fwd_gather(const FrontD *__restrict__ fr, const int32_t *__res
     }
 }
 
-// Forward gather of one front into ws (nrhs x ld_ws): w = b on the pivots
-// (zero on the boundary), plus child 0's update, plus child 1's, added in
+// Forward gather of one front into ws (nrhs x ld_ws): w = s_in b on the
+// pivots (zero on the boundary), plus child 0's update, plus child 1's, added in
 // that order; inv0 / inv1 give each of the front's rows its row in the
 // children's update blocks (or -1).  Threads t, t + nt, ... of the caller.
 template <typename T>
 __device__ __forceinline__ void gather_front(const FrontD *__restrict__ fr, const FrontD &f,
                                              const int32_t *__restrict__ v, const int32_t *__restrict__ inv0,
                                              const int32_t *__restrict__ inv1, const double2 *__restrict__ b,
-                                             const T *W, int64_t sum_m, int64_t n, int nrhs, T *ws, int ld_ws, int t,
+                                             const double *__restrict__ s_in, const T *W, int64_t sum_m, int64_t n,
+                                             int nrhs, T *ws, int ld_ws, int t,
                                              int nt) {
     const int64_t u0 = f.c0 >= 0 ? (int64_t)fr[f.c0].voff + fr[f.c0].p : 0;
     const int64_t u1 = f.c1 >= 0 ? (int64_t)fr[f.c1].voff + fr[f.c1].p : 0;
@@ -1132,7 +1133,7 @@ __device__ __forceinline__ void gather_front(const FrontD *__restrict__ fr, cons
         const int a0 = f.c0 >= 0 ? inv0[f.voff + k] : -1, a1 = f.c1 >= 0 ? inv1[f.voff + k] : -1;
         const int var = k < f.p ? v[k] : 0;
         for (int r = 0; r < nrhs; ++r) {
-            T w = (k < f.p) ? from_c128<T>(b[r * n + var], 1.0) : czero<T>();
+            T w = (k < f.p) ? from_c128<T>(b[r * n + var], s_in[r]) : czero<T>();
             if (a0 >= 0) w = cadd(w, W[r * sum_m + u0 + a0]);
             if (a1 >= 0) w = cadd(w, W[r * sum_m + u1 + a1]);
             ws[r * ld_ws + k] = w;
@@ -1188,8 +1189,8 @@ template <typename T>
 __global__ void __launch_bounds__(kSmallThreads)
     k_fwd_small(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0,
                 const int32_t *__restrict__ inv1,
-                const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
-                int nrhs, int f_begin, int maxm) {
+                const T *__restrict__ pool, const double2 *__restrict__ b, const double *__restrict__ s_in, T *W,
+                T *Y, int64_t sum_m, int64_t n, int nrhs, int f_begin, int maxm) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *ws = reinterpret_cast<T *>(smem_raw);   // [rhs][maxm]
     T *tmp = ws + (size_t)nrhs * maxm;          // [maxm]
@@ -1197,7 +1198,7 @@ __global__ void __launch_bounds__(kSmallThreads)
     const FrontD f = fr[f_begin + blockIdx.x];
     const int32_t *v = vars + f.voff;
     const int tid = threadIdx.x;
-    gather_front(fr, f, v, inv0, inv1, b, W, sum_m, n, nrhs, ws, maxm, tid, blockDim.x);
+    gather_front(fr, f, v, inv0, inv1, b, s_in, W, sum_m, n, nrhs, ws, maxm, tid, blockDim.x);
     __syncthreads();
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
@@ -1358,8 +1359,8 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kWarpFronts, sizeof(T) == 8 ? 5 : 4)
     k_fwd_warp(const FrontD *__restrict__ fr, const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0,
                const int32_t *__restrict__ inv1,
-               const T *__restrict__ pool, const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n,
-               int nrhs, int f_begin, int nfl, int maxm, int blocked) {
+               const T *__restrict__ pool, const double2 *__restrict__ b, const double *__restrict__ s_in, T *W,
+               T *Y, int64_t sum_m, int64_t n, int nrhs, int f_begin, int nfl, int maxm, int blocked) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int fi = blockIdx.x * kWarpFronts + warp;
@@ -1368,7 +1369,7 @@ __global__ void __launch_bounds__(32 * kWarpFronts, sizeof(T) == 8 ? 5 : 4)
     const FrontD f = fr[f_begin + fi];
     const int32_t *v = vars + f.voff;
     const int p = f.p, m = f.m;
-    gather_front(fr, f, v, inv0, inv1, b, W, sum_m, n, nrhs, ws, maxm, lane, 32);
+    gather_front(fr, f, v, inv0, inv1, b, s_in, W, sum_m, n, nrhs, ws, maxm, lane, 32);
     __syncwarp();
     const T *F = pool + f.f_off;
     const int64_t ld = f.ld;
@@ -2411,12 +2412,13 @@ template <typename T, typename R, int NR>
 __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
     k_fwd_level(const FrontD *__restrict__ fr, int fb, int nfl, int maxp, int maxm, const T *__restrict__ pool,
                 const int32_t *__restrict__ vars, const int32_t *__restrict__ inv0, const int32_t *__restrict__ inv1,
-                const double2 *__restrict__ b, T *W, T *Y, int64_t sum_m, int64_t n, int nrhs, GridBar *gb,
-                int *err, const int2 *__restrict__ units, int nunits, unsigned bar_limit, unsigned flag_limit) {
+                const double2 *__restrict__ b, const double *__restrict__ s_in, T *W, T *Y, int64_t sum_m,
+                int64_t n, int nrhs, GridBar *gb, int *err, const int2 *__restrict__ units, int nunits,
+                unsigned bar_limit, unsigned flag_limit) {
     if (NR == 1) nrhs = 1;  // one right-hand side: the sums stay in registers
     extern __shared__ unsigned char smem_raw[];
     const int tid = threadIdx.x;
-    // gather, spread over every CTA (one entry a thread): w = b on the
+    // gather, spread over every CTA (one entry a thread): w = s_in b on the
     // pivots (zero on the boundary), plus child 0's update, plus child 1's
     // -- the inverse maps give each parent row its children's update rows --
     // added in that order; the pivot slots of Y are marked unpublished
@@ -2430,7 +2432,7 @@ __global__ void __launch_bounds__(kRowsPerCta, sizeof(T) == 8 ? 3 : 1)
         const int64_t o1 = a1 >= 0 ? (int64_t)fr[f.c1].voff + fr[f.c1].p + a1 : 0;
         const int var = k < f.p ? vars[f.voff + k] : 0;
         for (int r = 0; r < nrhs; ++r) {
-            T v = (k < f.p) ? from_c128<T>(b[r * n + var], 1.0) : czero<T>();
+            T v = (k < f.p) ? from_c128<T>(b[r * n + var], s_in[r]) : czero<T>();
             if (a0 >= 0) v = cadd(v, W[r * sum_m + o0]);
             if (a1 >= 0) v = cadd(v, W[r * sum_m + o1]);
             W[r * sum_m + f.voff + k] = v;
@@ -2622,7 +2624,7 @@ bool small_level_fits(int maxp, int maxm, int nrhs) {
 }
 
 template <typename T, typename R>
-int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaStream_t st) {
+int solve_levels(fdfd_factor *fac, const double2 *b, const double *s_in, double2 *x, int nrhs, cudaStream_t st) {
     const Symbolic &S = fac->sym->s;
     T *W = (T *)fac->d_W, *Y = (T *)fac->d_Y;
     const T *pool = (const T *)fac->d_pool;
@@ -2642,8 +2644,9 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
             unsigned bar_limit = bar_limit_of(fac), flag_limit = flag_limit_of(fac);
             const int32_t *inv0 = fac->d_inv, *inv1 = fac->d_inv + S.sum_m;
             void *args[] = {(void *)&fac->d_fronts, (void *)&fb, (void *)&nfl, (void *)&maxp, (void *)&maxm,
-                            (void *)&pool, (void *)&fac->d_vars, (void *)&inv0, (void *)&inv1, (void *)&b, (void *)&W,
-                            (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs, (void *)&gb, (void *)&err,
+                            (void *)&pool, (void *)&fac->d_vars, (void *)&inv0, (void *)&inv1, (void *)&b,
+                            (void *)&s_in, (void *)&W, (void *)&Y, (void *)&sum_m, (void *)&n, (void *)&nrhs,
+                            (void *)&gb, (void *)&err,
                             (void *)&units, (void *)&nunits, (void *)&bar_limit, (void *)&flag_limit};
             // grid: the most work items any phase of this level has, capped
             // at the co-resident limit
@@ -2657,20 +2660,20 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
         const int maxm = S.lev_max_m[L], maxp = S.lev_max_p[L];
         if (warp_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_warp<T><<<(nfl + kWarpFronts - 1) / kWarpFronts, 32 * kWarpFronts, warp_smem_bytes<T>(nrhs, maxm),
-                            st>>>(fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, W, Y, sum_m,
-                                  n, nrhs, fb, nfl, maxm, (int)fac->blocked_level[L]);
+                            st>>>(fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, s_in, W, Y,
+                                  sum_m, n, nrhs, fb, nfl, maxm, (int)fac->blocked_level[L]);
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
         if (small_level_fits<T>(maxp, maxm, nrhs)) {
             k_fwd_small<T><<<nfl, kSmallThreads, small_smem_bytes<T>(nrhs, maxm), st>>>(
-                fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, W, Y, sum_m, n, nrhs, fb,
-                maxm);
+                fac->d_fronts, fac->d_vars, fac->d_inv, fac->d_inv + S.sum_m, pool, b, s_in, W, Y, sum_m, n, nrhs,
+                fb, maxm);
             prof_end(PROF_SOLVE_FWD, st, 1);
             continue;
         }
-        k_fwd_gather<T><<<nfl, 256, 0, st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, b, fac->d_unit,
-                                             W, sum_m, n, nrhs, fb);
+        k_fwd_gather<T><<<nfl, 256, 0, st>>>(fac->d_fronts, fac->d_vars, fac->d_relmap, b, s_in, W, sum_m, n,
+                                             nrhs, fb);
         int nl = 1;
         for (int k0 = 0; k0 < maxp; k0 += NB, ++nl) {
             const int rows = std::max(1, (maxm - k0 + kItemRows - 1) / kItemRows);
@@ -2760,19 +2763,38 @@ int solve_levels(fdfd_factor *fac, const double2 *b, double2 *x, int nrhs, cudaS
 namespace fdfd {
 namespace {
 
+// out[r] = s[r] in[r] for the nrhs columns of n entries.
 __global__ void k_colscale(const double2 *in, double2 *out, const double *s, int64_t n, int nrhs) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n * nrhs;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
-        const double c = s[k / n];
-        const double2 v = in[k];
-        out[k] = make_double2(v.x * c, v.y * c);
+        for (int r = 0; r < nrhs; ++r) {
+            const double c = s[r];
+            const double2 v = in[(size_t)r * n + k];
+            out[(size_t)r * n + k] = make_double2(__dmul_rn(v.x, c), __dmul_rn(v.y, c));
+        }
+    }
+}
+
+// acc[r] += s[r] v[r], rounded as the scaling and the sum done apart.
+__global__ void k_colscale_add(const double2 *v, double2 *acc, const double *s, int64_t n, int nrhs) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        for (int r = 0; r < nrhs; ++r) {
+            const double c = s[r];
+            const double2 a = acc[(size_t)r * n + k], b = v[(size_t)r * n + k];
+            acc[(size_t)r * n + k] =
+                make_double2(__dadd_rn(a.x, __dmul_rn(b.x, c)), __dadd_rn(a.y, __dmul_rn(b.y, c)));
+        }
     }
 }
 
 // One application of the factor on device vectors (no host sync):
 // out = A^-1 in  (transpose = 0) or A^-T in (transpose = 1).
+// have_norms: fac->d_norm already holds the nrhs column norms of `in`
+// (no transpose).  acc != NULL (no transpose): acc += A^-1 in instead, with
+// `out` as the scratch of the solve.
 int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, int transpose,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool have_norms = false, double2 *acc = nullptr) {
     const int64_t n = fac->n;
     if (transpose && !fac->has_p)
         return fail(FDFD_ERR_BAD_ARG, "transposed solve needs the operator's PML factors");
@@ -2783,20 +2805,24 @@ int apply_factor(fdfd_factor *fac, const double2 *in, double2 *out, int nrhs, in
                                                   nrhs, 0);
         src = tmp;
     }
+    if (transpose) have_norms = false, acc = nullptr;
     // scales from the column norms of the right-hand side
     prof_begin(PROF_OTHER, st);
-    int rc = norms_device(src, n, nrhs, fac->d_partial, fac->d_norm, st);
+    int rc = have_norms ? FDFD_OK : norms_device(src, n, nrhs, fac->d_partial, fac->d_norm, st);
     if (rc) return rc;
     k_scales<<<1, 32, 0, st>>>(fac->d_norm, fac->d_maxdiag, nrhs, fac->d_sin, fac->d_sout);
-    k_colscale<<<grid1(n * nrhs), 256, 0, st>>>(src, tmp, fac->d_sin, n, nrhs);
-    prof_end(PROF_OTHER, st, 4 + (transpose ? 1 : 0));
+    prof_end(PROF_OTHER, st, (have_norms ? 1 : 3) + (transpose ? 1 : 0));
+    // the forward gathers read src scaled by s_in
     if (fac->precision != FDFD_PREC_C128)
-        rc = solve_levels<c64, float>(fac, tmp, out, nrhs, st);
+        rc = solve_levels<c64, float>(fac, src, fac->d_sin, out, nrhs, st);
     else
-        rc = solve_levels<c128, double>(fac, tmp, out, nrhs, st);
+        rc = solve_levels<c128, double>(fac, src, fac->d_sin, out, nrhs, st);
     if (rc) return rc;
     prof_begin(PROF_OTHER, st);
-    k_colscale<<<grid1(n * nrhs), 256, 0, st>>>(out, out, fac->d_sout, n, nrhs);
+    if (acc)
+        k_colscale_add<<<grid1(n), 256, 0, st>>>(out, acc, fac->d_sout, n, nrhs);
+    else
+        k_colscale<<<grid1(n), 256, 0, st>>>(out, out, fac->d_sout, n, nrhs);
     prof_end(PROF_OTHER, st, 1 + (transpose ? 1 : 0));
     if (transpose)
         k_pscale<<<grid1(n * nrhs), 256, 0, st>>>(out, out, fac->d_isxf, fac->d_isyf, fac->Nx, fac->Ny,
@@ -3336,11 +3362,19 @@ static int refine_loop(fdfd_factor *fac, const OpDev &o, const double2 *bb, doub
             worst = std::max(worst, rel);
         }
         if (!(worst > tol) || it >= max_iter) break;
-        rc = apply_factor(fac, fac->d_r, fac->d_d, nrhs, transpose, st);
-        if (rc) return rc;
-        prof_begin(PROF_OTHER, st);
-        k_axpy<<<grid1(n * nrhs), 256, 0, st>>>(xx, fac->d_d, n * nrhs);
-        prof_end(PROF_OTHER, st, 1);
+        // x += M^-1 r: d_norm holds the residual's column norms when the
+        // segments are the columns; the correction is added by the
+        // solve's final scaling (no transpose)
+        if (transpose) {
+            rc = apply_factor(fac, fac->d_r, fac->d_d, nrhs, transpose, st);
+            if (rc) return rc;
+            prof_begin(PROF_OTHER, st);
+            k_axpy<<<grid1(n * nrhs), 256, 0, st>>>(xx, fac->d_d, n * nrhs);
+            prof_end(PROF_OTHER, st, 1);
+        } else {
+            rc = apply_factor(fac, fac->d_r, fac->d_d, nrhs, 0, st, seg == n && nseg == nrhs, xx);
+            if (rc) return rc;
+        }
         ++it;
     }
     CUDA_TRY(cudaEventRecord(fac->ev[3], st));
