@@ -61,6 +61,34 @@ def to_host(*ts):
     return [h.numpy() for h in hs]
 
 
+_copy_streams: dict = {}
+
+
+def to_host_start(t):
+    """Start the device -> host copy of t into a page-locked buffer on a
+    side stream, after the work queued so far on the current stream, so
+    that it runs beside the kernels queued next (t must not be written by
+    them).  to_host_finish returns the numpy array."""
+    cur = torch.cuda.current_stream()
+    st = _copy_streams.get(cur.device)
+    if st is None:
+        st = _copy_streams.setdefault(cur.device, torch.cuda.Stream(device=cur.device))
+    st.wait_stream(cur)
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    with torch.cuda.stream(st):
+        h.copy_(t, non_blocking=True)
+    t.record_stream(st)
+    ev = torch.cuda.Event()
+    ev.record(st)
+    return h, ev
+
+
+def to_host_finish(pending):
+    h, ev = pending
+    ev.synchronize()
+    return h.numpy()
+
+
 def as_f64(x) -> torch.Tensor:
     dev = device()
     if isinstance(x, torch.Tensor):

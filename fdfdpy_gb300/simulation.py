@@ -221,13 +221,15 @@ class Simulation:
             eps_dev = self._op.eps + self._eps_nl_device()[0]
         else:
             eps_dev = self._op.eps if self.pol == 'Hz' else None
+        # the primary field goes to the host while the other two are derived
+        pending = None if zero_src else engine.to_host_start(X)
         f1, f2 = self._op.fields(X, averaging=averaging, eps=eps_dev)
+        F1, F2 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2))
         if zero_src:
             # an all-zero source gives float zeros for the primary field (linalg.py:128-129)
-            F1, F2 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2))
             F3 = np.zeros((Nx, Ny))
         else:
-            F1, F2, F3 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2, X))
+            F3 = engine.to_host_finish(pending).reshape((Nx, Ny))
         if timing:
             print('Linear system solve took {:.2f} seconds'.format(time() - t))
         # device copies of the fields, tied to the host arrays returned now
