@@ -169,9 +169,15 @@ __global__ void __launch_bounds__(kCoefCols) k_coef(OpDev o, double2 *coef, int6
 }
 
 // max |A[k,k]| over the grid, as the bit pattern of a non-negative double.
+// hypot (many FP64 operations on this GPU) is evaluated once a thread, for
+// the entry of largest squared modulus, and for the entries within 1e-12
+// of that one's squared modulus that differ from it; an entry outside the
+// margin has a smaller hypot than the kept one (the rounding of both is far
+// below 1e-12), so the result is the maximum of hypot over every entry.
 __global__ void k_maxdiag(OpDev o, unsigned long long *out) {
     const int64_t n = (int64_t)o.Nx * o.Ny;
-    double mx = 0.0;
+    double mx = 0.0, s2max = -1.0;  // no entry kept yet
+    double2 best = make_double2(0.0, 0.0);
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
          k += (int64_t)gridDim.x * blockDim.x) {
         double2 c0;
@@ -182,8 +188,15 @@ __global__ void k_maxdiag(OpDev o, unsigned long long *out) {
             stencil_row(o, (int)(k / o.Ny), (int)(k % o.Ny), c);
             c0 = c[0];
         }
-        mx = fmax(mx, hypot(c0.x, c0.y));
+        const double s2 = c0.x * c0.x + c0.y * c0.y;
+        if (s2 > s2max * (1.0 + 1e-12)) {
+            best = c0;  // a clearly larger entry: the previous one cannot be the maximum
+            s2max = s2;
+        } else if (!(s2 < s2max * (1.0 - 1e-12)) && (c0.x != best.x || c0.y != best.y)) {
+            mx = fmax(mx, hypot(c0.x, c0.y));  // within the margin (or NaN): evaluated
+        }
     }
+    if (s2max >= 0.0) mx = fmax(mx, hypot(best.x, best.y));
     for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
     if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
 }
@@ -2043,7 +2056,7 @@ int factor_levels(fdfd_factor *fac, const OpDev &o, cudaStream_t st) {
     if (fac->d_tcerr) CUDA_TRY(cudaMemsetAsync(fac->d_tcerr, 0, sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(fac->d_maxdiag, 0, sizeof(unsigned long long), st));
     prof_begin(PROF_ASSEMBLE, st);
-    k_maxdiag<<<grid1(fac->n), 256, 0, st>>>(o, fac->d_maxdiag);
+    k_maxdiag<<<std::min(grid1(fac->n), 152 * 4), 256, 0, st>>>(o, fac->d_maxdiag);  // many entries a thread
     if (!leaf_asm)
         k_assemble_fronts<T><<<grid1(fac->n), 256, 0, st>>>(o, fac->d_fronts, fac->d_vfront, fac->d_vloc, fac->d_nbr,
                                                            fac->d_maxdiag, (T *)fac->d_pool, 0, S.level_ptr[1]);
