@@ -51,28 +51,29 @@ def to_host(*ts):
     """Device tensors -> numpy arrays through page-locked buffers from
     torch's caching host allocator (the copies run at link speed, with no
     staging copy on the host; a buffer is reused once the caller has dropped
-    an earlier result).  One synchronisation for all of them."""
-    hs = []
-    for t in ts:
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        h.copy_(t, non_blocking=True)
-        hs.append(h)
-    torch.cuda.current_stream().synchronize()
-    return [h.numpy() for h in hs]
+    an earlier result).  Each tensor's copy runs on its own copy stream, so
+    that several copies share the link at once."""
+    pending = [to_host_start(t, slot=i) for i, t in enumerate(ts)]
+    return [to_host_finish(p) for p in pending]
 
 
 _copy_streams: dict = {}
+_copy_lock = threading.Lock()
 
 
-def to_host_start(t):
-    """Start the device -> host copy of t into a page-locked buffer on a
-    side stream, after the work queued so far on the current stream, so
-    that it runs beside the kernels queued next (t must not be written by
-    them).  to_host_finish returns the numpy array."""
+def to_host_start(t, slot=0):
+    """Start the device -> host copy of t into a page-locked buffer on copy
+    stream `slot` (of a few per device), after the work queued so far on the
+    current stream, so that it runs beside the kernels queued next (t must
+    not be written by them).  to_host_finish returns the numpy array."""
     cur = torch.cuda.current_stream()
-    st = _copy_streams.get(cur.device)
-    if st is None:
-        st = _copy_streams.setdefault(cur.device, torch.cuda.Stream(device=cur.device))
+    # copy streams of the caller's stream: callers on other streams (the
+    # serving slots) do not queue behind each other's copies
+    with _copy_lock:
+        pool = _copy_streams.setdefault((cur.device, cur.cuda_stream), [])
+        while len(pool) <= slot:
+            pool.append(torch.cuda.Stream(device=cur.device))
+        st = pool[slot]
     st.wait_stream(cur)
     h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
     with torch.cuda.stream(st):

@@ -222,7 +222,7 @@ class Simulation:
         else:
             eps_dev = self._op.eps if self.pol == 'Hz' else None
         # the primary field goes to the host while the other two are derived
-        pending = None if zero_src else engine.to_host_start(X)
+        pending = None if zero_src else engine.to_host_start(X, slot=2)
         f1, f2 = self._op.fields(X, averaging=averaging, eps=eps_dev)
         F1, F2 = (a.reshape((Nx, Ny)) for a in engine.to_host(f1, f2))
         if zero_src:
