@@ -481,7 +481,7 @@ def run_adjoint(args):
 
 def run_peaks(args):
     """Peak arithmetic rates of this GPU for the roofline denominators that
-    the driver does not measure: cuBLAS GEMMs (torch.matmul) of 8192^3 in
+    the measured-peaks file does not hold: cuBLAS GEMMs (torch.matmul) of 8192^3 in
     float32 with TF32 tensor cores, float32 without them (FFMA), and float64
     (DFMA / FP64 pipe); best of 10 back-to-back launches timed with CUDA
     events.  Also a device-to-device copy (read + write bytes)."""
