@@ -70,6 +70,8 @@ def to_host_start(t, slot=0):
     # copy streams of the caller's stream: callers on other streams (the
     # serving slots) do not queue behind each other's copies
     with _copy_lock:
+        if len(_copy_streams) > 64:
+            _copy_streams.clear()  # callers that come and go: torch's streams are pooled, none is destroyed
         pool = _copy_streams.setdefault((cur.device, cur.cuda_stream), [])
         while len(pool) <= slot:
             pool.append(torch.cuda.Stream(device=cur.device))
