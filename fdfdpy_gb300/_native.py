@@ -99,6 +99,7 @@ SIGNATURES = {
     "fdfd_factor_numeric_batch": (C.c_int, [P, POP, I32, P]),
     "fdfd_solve_refined_batch": (C.c_int, [P, P, P, I32, D, I32, P, P]),
     "fdfd_factor_stats_get": (C.c_int, [P, C.POINTER(FactorStats)]),
+    "fdfd_factor_coef_get": (C.c_int, [P, P, P]),
     "fdfd_factor_set_pivot_tol": (C.c_int, [P, D]),
     "fdfd_factor_set_fused_limit": (C.c_int, [P, I32]),
     "fdfd_factor_set_wait_limit": (C.c_int, [P, I64]),

@@ -3627,6 +3627,16 @@ extern "C" int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const
     return FDFD_OK;
 }
 
+extern "C" int fdfd_factor_coef_get(const fdfd_factor *fac, void *dst, void *stream) {
+    if (!fac || !dst) return fail(FDFD_ERR_BAD_ARG, "factor_coef_get: NULL argument");
+    if (!fac->coef_valid)
+        return fail(FDFD_ERR_BAD_ARG, "factor_coef_get: no stored coefficients (a numeric factorization of an "
+                                      "operator given by eps and the 1/s vectors comes first)");
+    CUDA_TRY(cudaMemcpyAsync(dst, fac->d_coef, (size_t)5 * fac->n * 16, cudaMemcpyDeviceToDevice,
+                             (cudaStream_t)stream));
+    return FDFD_OK;
+}
+
 extern "C" int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st) {
     if (!fac || !st) return fail(FDFD_ERR_BAD_ARG, "factor_stats: NULL argument");
     fdfd_factor *f = const_cast<fdfd_factor *>(fac);

@@ -426,6 +426,15 @@ class Factor:
         self._last = (worst, iters)
         return torch.cat(outs).reshape(b.shape)
 
+    def coefficients(self) -> torch.Tensor:
+        """The operator coefficients the last numeric factorization stored,
+        complex128 (5, n): centre, (i-1, j), (i+1, j), (i, j-1), (i, j+1)
+        of cell k = i Ny + j (fdfd_factor_coef_get)."""
+        out = torch.empty(5, self.sym.Nx * self.sym.Ny, dtype=torch.complex128,
+                          device=device())
+        N.call("fdfd_factor_coef_get", self.handle, _ptr(out), stream_ptr())
+        return out
+
     def stats(self) -> dict:
         """Counters of the last factorization and solve (the residual and
         refinement count are the worst over the column blocks of the last

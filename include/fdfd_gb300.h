@@ -358,6 +358,14 @@ int fdfd_solve_gmres(fdfd_factor *fac, const fdfd_operator *op, const void *b,
                      void *x, int32_t transpose, double tol, int32_t max_iter,
                      int32_t restart, void *stream);
 int fdfd_factor_stats_get(const fdfd_factor *fac, fdfd_factor_stats *st);
+/* Copies the factor's stored operator coefficients, complex128 [5][n]
+ * (the centre, then the (i-1, j), (i+1, j), (i, j-1), (i, j+1) neighbours
+ * of cell k = i Ny + j; n = Nx Ny), into dst (device memory, 80 n bytes),
+ * ordered on `stream`.  Valid after fdfd_factor_numeric of an operator
+ * given by eps and the 1/s vectors (not an explicit stencil), else
+ * FDFD_ERR_BAD_ARG.  For tests and diagnostics: the entries are those of
+ * row k of construct_A (fdfd_assemble_csr).  No counterpart in fdfdpy. */
+int fdfd_factor_coef_get(const fdfd_factor *fac, void *dst, void *stream);
 void fdfd_factor_destroy(fdfd_factor *fac);
 
 /* ---- profiling -----------------------------------------------------------

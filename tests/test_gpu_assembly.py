@@ -164,3 +164,41 @@ def test_bad_arguments_raise(eng):
     op = N.Operator()
     op.Nx, op.Ny, op.pol = 4, 4, 0
     assert N.lib().fdfd_assemble_csr(C.byref(op), None, None, None, None) == N.FDFD_ERR_BAD_ARG
+
+
+@pytest.mark.parametrize("shape,pol,averaging,kerr", [
+    ((48, 40, 0.02, (8, 6)), "Ez", True, False),
+    ((48, 40, 0.02, (8, 6)), "Hz", True, True),
+    ((37, 300, 0.01, (5, 20)), "Hz", True, False),
+    ((37, 300, 0.01, (5, 20)), "Hz", False, True),
+    ((100, 513, 0.01, (10, 10)), "Ez", True, True),
+    ((257, 256, 0.01, (20, 20)), "Hz", True, False),
+])
+def test_factor_coefficients_equal_construct_A(eng, shape, pol, averaging, kerr):
+    """The coefficient store a factorization evaluates (k_coef: tiled, the
+    sign-symmetric forms, 1/eps shared between neighbouring cells) holds
+    exactly the entries of construct_A's rows (K1, cell by cell), in every
+    direction, with ragged column blocks, both polarizations, with and
+    without averaging and a Kerr term."""
+    Nx, Ny, dl, npml = shape
+    rng = np.random.default_rng(Nx * Ny)
+    eps = np.kron(rng.choice([1.0, 12.25], size=(-(-Nx // 4), -(-Ny // 4))), np.ones((4, 4)))[:Nx, :Ny]
+    eps_add = torch.from_numpy(rng.random((Nx, Ny))).cuda() if kerr else None
+    op = eng.DeviceOperator(OMEGA, eps, Nx * dl, Ny * dl, list(npml), pol, 1e-6, averaging=averaging,
+                            eps_add=eps_add)
+    indptr, indices, data = op.csr_device()
+    fac = eng.Factor(eng.symbolic_for(Nx, Ny), "c64").numeric(op)
+    coef = fac.coefficients()
+    n = Nx * Ny
+    k = torch.arange(n, device=coef.device)
+    i, j = k // Ny, k % Ny
+    cols = torch.stack([k, ((i - 1) % Nx) * Ny + j, ((i + 1) % Nx) * Ny + j, i * Ny + (j - 1) % Ny,
+                        i * Ny + (j + 1) % Ny])
+    assert torch.equal(indptr[1:] - indptr[:-1], torch.full((n,), 5, dtype=indptr.dtype, device=indptr.device))
+    idx2 = indices.reshape(n, 5).long()
+    dat2 = data.reshape(n, 5)
+    for d in range(5):
+        hit = idx2 == cols[d][:, None]
+        assert torch.equal(hit.sum(1), torch.ones(n, dtype=hit.sum(1).dtype, device=hit.device))
+        want = dat2[hit]
+        assert torch.equal(coef[d], want), f"direction {d}: {int((coef[d] != want).sum())} entries differ"
