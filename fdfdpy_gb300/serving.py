@@ -43,7 +43,7 @@ import torch
 from . import engine
 
 
-@dataclass
+@dataclass(eq=False)  # a request is equal only to itself (the queue looks requests up by identity)
 class Request:
     eps_r: np.ndarray
     rhs: np.ndarray               # (nrhs, Nx*Ny) complex128 right-hand sides b
