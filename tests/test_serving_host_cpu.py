@@ -90,3 +90,87 @@ def test_dispatch_admits_by_memory_and_serves_every_request(make_server, monkeyp
     assert peak["batch"] == 2            # a batch of 4 (400 bytes) does not fit 250: cut to 2
     assert peak["resident"] <= s.budget
     assert s.resident == 0               # every unit gave its memory back
+
+
+class _Stream:
+    def synchronize(self):
+        pass
+
+
+class _FakeEngine:
+    """Factor / BatchFactor / DeviceOperator stand-ins that solve nothing:
+    x = b, a residual chosen per operator, and a factorization that fails
+    for 12 x 12 grids."""
+
+    def __init__(self, bad_residual_keys):
+        eng = self
+
+        class DeviceOperator:
+            def __init__(self, omega, eps_r, xlen, ylen, NPML, pol, L0):
+                self.eps_r = eps_r
+
+        class Factor:
+            def __init__(self, sym, precision, max_nrhs=8, fused_max_m=None):
+                self.precision = precision
+
+            def numeric(self, op):
+                if op.eps_r.shape == (12, 12):
+                    raise RuntimeError("factor_create: device allocation failed")
+                self.op = op
+                return self
+
+            def solve(self, b, tol, max_iter, op=None):
+                bad = self.precision != "c128" and eng.key(op.eps_r) in bad_residual_keys
+                self._st = {"rel_residual": 1e-3 if bad else 1e-12, "refine_iters": 3}
+                return b.clone()
+
+            def stats(self):
+                return self._st
+
+        class BatchFactor:
+            def __init__(self, sym, precision, max_nrhs=8, fused_max_m=None):
+                self.batch = sym[2]
+
+            def numeric(self, ops):
+                self.ops = ops
+                return self
+
+            def solve_batch(self, rhs, tol, max_iter):
+                return [b.clone() for b in rhs], [1e-12] * len(rhs)
+
+            def stats(self):
+                return {"refine_iters": 2}
+
+        self.DeviceOperator, self.Factor, self.BatchFactor = DeviceOperator, Factor, BatchFactor
+
+    @staticmethod
+    def key(eps):
+        return eps.tobytes()
+
+
+def test_serve_caches_reuses_falls_back_and_accounts_memory(make_server, monkeypatch):
+    """The real per-unit path (_serve / _solve_on) over fake engine objects,
+    one slot: a repeated operator is a cache hit on the entry its first
+    request built, a request whose complex64 refinement stalls is solved
+    again in complex128, a factorization that fails fails its requests only,
+    and the resident bytes are exactly those of the cached entries."""
+    reqs = [_req(1), _req(2), _req(1), _req(3, shape=(12, 12)), _req(4), _req(4, nrhs=3)]
+    fake = _FakeEngine({_FakeEngine.key(reqs[4].eps_r)})
+    monkeypatch.setattr(serving.engine, "DeviceOperator", fake.DeviceOperator)
+    monkeypatch.setattr(serving.engine, "Factor", fake.Factor)
+    monkeypatch.setattr(serving.engine, "BatchFactor", fake.BatchFactor)
+    monkeypatch.setattr(torch.cuda, "Stream", lambda *a, **k: _Stream())
+    monkeypatch.setattr(torch.cuda, "stream", lambda s: __import__("contextlib").nullcontext())
+    s = make_server(budget=10_000, batch_max=1, slots=1)
+    s._sym = lambda shape, batch=1: (shape[0], shape[1], batch)
+    s._need = lambda shape, batch=1: 100 * batch
+    out = s.run(reqs, realtime=False)
+    assert reqs[3].error is not None and "device allocation failed" in reqs[3].error
+    ok = [r for i, r in enumerate(reqs) if i != 3]
+    assert all(r.error is None and r.x is not None for r in ok)
+    assert [r.cache_hit for r in reqs] == [False, False, True, False, False, True]
+    assert np.array_equal(reqs[5].x, reqs[5].rhs)            # x = b from the fake factor
+    assert reqs[4].fallback and reqs[5].fallback and not reqs[0].fallback
+    assert out["factorizations"] == 3 and out["failed"] == 1 and out["cache_hits"] == 2
+    assert s.resident == sum(e.bytes for e in s.cache.values()) == 300
+    assert all(e.users == 0 for e in s.cache.values())
